@@ -1,0 +1,217 @@
+/*
+ * instaheat_gpu.h -- C ABI of libinstaheat_gpu.so, the GB300 (sm_103a)
+ * implementation of InstaHeat's right-hand side and time steppers.
+ *
+ * Every entry point takes plain pointers and sizes, returns an int status
+ * (IH_OK = 0, see ih_status_string) instead of calling exit(), and is called
+ * from one host thread per context.  One context owns one grid on one GPU:
+ * its device-resident state, the DOPRI853/RK4 work vectors, the k grids, the
+ * filter mask and the FFT tables.
+ *
+ * State layout (host side, identical to the reference, src/main_template.h:
+ * 223-233): f[Ntot], Ntot = 4N + 4Next + 1: phi, dphi, psi, dpsi (N doubles
+ * each, row-major [x][y][z]), h1, h2, dh1, dh2 (Next = 2M doubles each, M
+ * interleaved complex, r2c half spectrum [x][y][z/2+1]), then a.
+ *
+ * Precision forms:
+ *   IH_PREC_F64   -- plain FP64 everywhere (the reference's arithmetic).
+ *   IH_PREC_MIXED -- FP32 fluctuation fields, FFTs and pointwise arithmetic;
+ *                    FP64 homogeneous (k = 0) parts of phi, dphi, psi, dpsi,
+ *                    FP64 scale factor a, Hubble rate, <rho>, <p>, all
+ *                    reductions and the DOPRI853 error norm.
+ *
+ * The drop-in symbols that the reference's own C code calls (mk_rhs,
+ * run_dopri853, run_rk4, fft, ifft, mean, variance, evo_flags) are provided by
+ * the C99 host layer declared in instaheat_dropin.h, on top of this ABI.
+ */
+#ifndef INSTAHEAT_GPU_H
+#define INSTAHEAT_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    IH_OK = 0,
+    IH_ERR_ARG = 1,        /* invalid argument or unsupported grid */
+    IH_ERR_CUDA = 2,       /* a CUDA call failed (message in ih_last_error) */
+    IH_ERR_ALLOC = 3,      /* device or host allocation failed */
+    IH_ERR_STATE = 4,      /* call out of order (e.g. step before init) */
+    IH_ERR_UNDERFLOW = 5,  /* DOPRI853 step-size underflow (dopri853.c:280-283) */
+    IH_ERR_NAN = 6         /* non-finite value in a reduction (NaN/Inf flag) */
+};
+
+enum { IH_PREC_F64 = 0, IH_PREC_MIXED = 1 };
+
+/* Grid and physics parameters: the parameters.sh keys of the hot path. */
+typedef struct {
+    int nx, ny, nz;        /* GRIDPOINTS_X/Y/Z: powers of two, nx >= ny >= nz >= 4 */
+    double lx, ly, lz;     /* SPATIAL_UPPER_BOUND_* - SPATIAL_LOWER_BOUND_* */
+    double mass;           /* MASS (V = m^2 phi^2 / 2) */
+    int enable_gw;         /* ENABLE_GW */
+    int enable_filter;     /* ENABLE_FFT_FILTER */
+    int bins;              /* POWER_SPECTRUM_BINS (field and GW spectra) */
+    int precision;         /* IH_PREC_F64 or IH_PREC_MIXED */
+    int device;            /* CUDA device ordinal */
+} ih_params;
+
+/* DOPRI853 controller parameters (parameters.sh: RELATIVE_TOLERANCE,
+ * ABSOLUTE_TOLERANCE, BETA, SAFE, SMALLEST_SCALING, LARGEST_SCALING,
+ * MAX_DT_HUBBLE_FRACTION (<= 0 disables the cap), MINIMAL_DELTA_T, MAX_STEPS). */
+typedef struct {
+    double rtol, atol, beta, safe, minscale, maxscale;
+    double max_dt_hubble_fraction, dt_min, max_steps;
+} ih_dopri_cfg;
+
+/* Diagnostics of the last RHS evaluated with the output flag
+ * (toolbox.c:251-270).  Arrays are caller-owned, `bins` doubles each; any
+ * pointer may be NULL. */
+typedef struct {
+    double *phi_ps, *psi_ps, *rho_ps, *gw;
+    double cstr[4];        /* <ham^2>, max|ham|, <mom^2>, max|mom| */
+    double smry[6][4];     /* phi, dphi, psi, dpsi, rho, p: mean, var, min, max */
+} ih_output;
+
+/* Result of one DOPRI853 perform_step (dopri853.c:271-311). */
+typedef struct {
+    double t;              /* time after the step */
+    double dt_did;         /* accepted step size */
+    double dt_next;        /* proposed next step size */
+    double err;            /* error() of the accepted try */
+    int tries;             /* try_step calls, rejected ones included */
+    int status;            /* IH_OK or IH_ERR_UNDERFLOW */
+} ih_step_info;
+
+const char *ih_status_string(int status);
+
+/* Sizes N, M, Next, Ntot of a grid (setup.c:228-271, 3D). */
+int ih_sizes(int nx, int ny, int nz, size_t *N, size_t *M, size_t *Next,
+             size_t *Ntot);
+
+typedef struct ih_context ih_context;
+
+/* Create a context (allocates all device memory for the grid; replaces
+ * allocate_external, setup.c:354-477, mk_k_grid 609-666, mk_filter_mask
+ * 710-754 and the FFTW plans 524-554). */
+int ih_create(const ih_params *p, ih_context **out);
+void ih_destroy(ih_context *c);
+const char *ih_last_error(const ih_context *c);
+/* Device bytes the context holds. */
+size_t ih_device_bytes(const ih_context *c);
+
+/* ---- state transfer (host FP64, reference layout) ---- */
+/* Upload `field` and set the time.  The DOPRI853 controller state is kept;
+ * ih_dopri853_step uses the dfield on the device, so a caller that replaces
+ * the state either uploads the matching dfield with ih_set_dstate or calls
+ * ih_dopri853_init (which recomputes it with the filtered RHS). */
+int ih_set_state(ih_context *c, const double *f_host, double t);
+int ih_get_state(ih_context *c, double *f_host);
+/* dfield: the RHS of the current state (valid after ih_dopri853_init/step). */
+int ih_set_dstate(ih_context *c, const double *df_host);
+int ih_get_dstate(ih_context *c, double *df_host);
+double ih_time(const ih_context *c);
+
+/* ---- the RHS (toolbox.c:75-88) ---- */
+/* mk_rhs on host buffers: uploads f, evaluates, downloads result.  With
+ * filter=1 (and ENABLE_FFT_FILTER) f is overwritten by its filtered version,
+ * as the reference does (toolbox.c:164-171).  With output=1 the diagnostics
+ * are computed and kept for ih_get_output. */
+int ih_mk_rhs_host(ih_context *c, double t, double *f, double *result,
+                   int filter, int output);
+/* mk_rhs on device pointers in the reference layout (FP64, Ntot doubles).
+ * f_dev is overwritten when filter=1.  Plain FP64 contexts only. */
+int ih_mk_rhs_dev(ih_context *c, double t, double *f_dev, double *result_dev,
+                  int filter, int output);
+/* <rho>, <p> of the last RHS (the reference's rho_mean, pressure_mean). */
+int ih_get_means(const ih_context *c, double *rho_mean, double *pressure_mean);
+/* Copy a per-point field of the last RHS to host (N doubles):
+ * which = 0 rho, 1 pressure, 2 laplacian of phi, 3 squared gradient. */
+int ih_get_field(ih_context *c, int which, double *out_host);
+int ih_get_output(ih_context *c, ih_output *out);
+unsigned long long ih_calls_rhs(const ih_context *c);
+
+/* ---- transforms (fft / ifft, toolbox.c:806-827) on host buffers ----
+ * r2c unnormalised exp(-i..) [x][y][z/2+1]; c2r unnormalised exp(+i..).
+ * Computed in the context's precision. */
+int ih_fft_host(ih_context *c, const double *in, double *out_c);
+int ih_ifft_host(ih_context *c, const double *in_c, double *out);
+
+/* ---- initial conditions ---- */
+/* Seeded fluctuations generated on the GPU: delta phi_k complex Gaussian with
+ * E|c_k|^2 = amp^2/(2 omega_k L^3), omega_k = sqrt(k^2 + m^2), zero for k = 0
+ * and |k| > kcut, Hermitian on the kz = 0 and kz = nz/2 planes; delta dphi_k =
+ * -i omega_k delta phi_k; phi = phi0 + delta phi, dphi = dphi0 + delta dphi,
+ * psi = dpsi = h = 0, a = a0.  The counter-based generator (SplitMix64 +
+ * Box-Muller) makes every mode a pure function of (seed, mode index). */
+int ih_ic_fluctuations(ih_context *c, uint64_t seed, double phi0,
+                       double dphi0, double a0, double amp, double kcut);
+/* mk_initial_psi (setup.c:825-903) on the device state. */
+int ih_initial_psi(ih_context *c);
+
+/* ---- DOPRI853 (dopri853.c) ---- */
+/* initialize_dopri853 + the first RHS with filter=1 (dopri853.c:172-198,
+ * toolbox.c:96-104). */
+int ih_dopri853_init(ih_context *c, const ih_dopri_cfg *cfg, double t0,
+                     double dt0);
+/* perform_step with dt_try; want_output=1 computes the diagnostics on the
+ * post-step RHS (dopri853.c:288-291). */
+int ih_dopri853_step(ih_context *c, double dt_try, int want_output,
+                     ih_step_info *info);
+/* The run loop (dopri853.c:112-158) to tf or max_steps accepted steps; if
+ * log is not NULL, 4 doubles (t, dt_did, err, tries) per accepted step are
+ * written up to log_cap steps.  *n_steps receives the accepted steps. */
+int ih_dopri853_run(ih_context *c, double tf, long max_steps, double *log,
+                    long log_cap, long *n_steps);
+/* Controller state: dt_next and the number of accepted/rejected steps. */
+int ih_dopri853_counters(const ih_context *c, double *dt_next, long *n_ok,
+                         long *n_bad, long *n_tries);
+/* Tableau (Hairer's DOP853 coefficients): c[12], a[12*12] row-major,
+ * b[12], bhh[3] (stages 1, 9, 12), er[12]. */
+int ih_dopri853_tableau(double *c, double *a, double *b, double *bhh,
+                        double *er);
+
+/* ---- RK4 (rk4.c:27-132) ---- */
+/* One step of size dt from the context time; the stage-1 RHS runs with
+ * filter=1 and, if want_output, output=1 (rk4.c:63-75). */
+int ih_rk4_step(ih_context *c, double dt, int want_output);
+
+/* Mixed form only: before an element of the two embedded error vectors enters
+ * the FP64 error norm, its FP32 rounding floor eta * 2^-24 * sum_j |c_j k_j|
+ * is subtracted from its magnitude (soft threshold), so that FP32 round-off
+ * in the stage vectors does not drive the step size down.  Default eta = 32
+ * in the mixed form; the plain FP64 form ignores it.  No reference
+ * counterpart (the reference is FP64 only). */
+int ih_dopri853_set_noise_floor(ih_context *c, double eta);
+
+/* ---- timing and instrumentation ---- */
+/* Synchronise the context's stream. */
+int ih_sync(ih_context *c);
+/* Device time (ms, CUDA events on the context stream) accumulated by the
+ * kernels of class `cls` since the last reset, and their launch count:
+ * cls 0 = all FFT passes, 1 = pointwise RHS kernels, 2 = stepper kernels. */
+int ih_profile_enable(ih_context *c, int on);
+int ih_profile_read(ih_context *c, int cls, double *ms, long *launches);
+/* The same per kernel kind (0 .. ih_profile_kernel_count()-1, named by
+ * ih_profile_kernel_name), with the algorithmic bytes of the timed launches
+ * (each input read once, each output written once). */
+int ih_profile_kernel(ih_context *c, int kind, double *ms, long *launches,
+                      double *bytes);
+const char *ih_profile_kernel_name(int kind);
+int ih_profile_kernel_count(void);
+/* CUDA-event timer on the context stream: start, then stop returns ms. */
+int ih_timer_start(ih_context *c);
+int ih_timer_stop(ih_context *c, double *ms);
+/* Kernel launches issued by this context since creation. */
+unsigned long long ih_kernel_launches(const ih_context *c);
+
+/* ---- pinned host memory for end-to-end transfers ---- */
+int ih_host_alloc(size_t bytes, void **out);
+int ih_host_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

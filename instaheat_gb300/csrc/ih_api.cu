@@ -1,0 +1,640 @@
+// ih_api.cu -- the extern "C" entry points of libinstaheat_gpu.so
+// (declared in include/instaheat_gpu.h) and the context lifecycle.
+#include <math.h>
+#include <string.h>
+#include <new>
+#include "ih_internal.cuh"
+
+namespace ih {
+
+int check_launch(Ctx *c, const char *what) {
+  c->launches += 1;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    c->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return IH_ERR_CUDA;
+  }
+  return IH_OK;
+}
+
+const char *kernel_kind_name(int k) {
+  static const char *names[KK_COUNT] = {
+      "k_fft_xy",       "k_fft_zr2c",    "k_fft_zc2r",       "k_fft_x_deriv4_inv",
+      "k_fft_z_rhs_fused", "k_update_h", "k_update_phi_psi", "k_filter_spectra",
+      "k_lincomb",      "k_dopri_final"};
+  return (k >= 0 && k < KK_COUNT) ? names[k] : "unknown";
+}
+
+int kernel_kind_class(int k) {
+  if (k <= KK_Z_RHS_FUSED) return 0;
+  if (k <= KK_FILTER) return 1;
+  return 2;
+}
+
+void prof_begin(Ctx *c, int kind) {
+  if (!c->prof_on) return;
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  cudaEventRecord(e, c->stream);
+  c->timers[kind].ev.push_back(e);
+}
+void prof_end(Ctx *c, int kind, double bytes) {
+  if (!c->prof_on) return;
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  cudaEventRecord(e, c->stream);
+  c->timers[kind].ev.push_back(e);
+  c->timers[kind].launches += 1;
+  c->timers[kind].bytes += bytes;
+}
+
+static bool pow2(int n) { return n >= 1 && (n & (n - 1)) == 0; }
+
+static int validate(const ih_params *p, std::string *why) {
+  if (!p) {
+    *why = "null parameters";
+    return IH_ERR_ARG;
+  }
+  if (!pow2(p->nx) || !pow2(p->ny) || !pow2(p->nz)) {
+    *why = "grid sizes must be powers of two";
+    return IH_ERR_ARG;
+  }
+  if (p->nx < p->ny || p->ny < p->nz) {
+    *why = "order number of gridpoints Nx >= Ny >= Nz (setup.c:219-222)";
+    return IH_ERR_ARG;
+  }
+  if (p->nz < 8) {
+    *why = "the 3D GPU path needs nz >= 8";
+    return IH_ERR_ARG;
+  }
+  const int zmax = p->precision == IH_PREC_MIXED ? 512 : 256;
+  if (p->nx > 512 || p->nz > zmax) {
+    *why = "grid too large for the shared-memory FFT tiles (nx <= 512; nz <= 256 in FP64, "
+           "<= 512 in the mixed form)";
+    return IH_ERR_ARG;
+  }
+  if (!(p->lx > 0 && p->ly > 0 && p->lz > 0)) {
+    *why = "box lengths must be positive";
+    return IH_ERR_ARG;
+  }
+  if (p->bins < 1) {
+    *why = "POWER_SPECTRUM_BINS must be positive";
+    return IH_ERR_ARG;
+  }
+  if (p->precision != IH_PREC_F64 && p->precision != IH_PREC_MIXED) {
+    *why = "unknown precision";
+    return IH_ERR_ARG;
+  }
+  return IH_OK;
+}
+
+static void make_geom(const ih_params *p, Geom *g) {
+  g->nx = p->nx;
+  g->ny = p->ny;
+  g->nz = p->nz;
+  g->h = p->nz / 2;
+  g->mz = p->nz / 2 + 1;
+  g->N = (long long)p->nx * p->ny * p->nz;
+  g->M = (long long)p->nx * p->ny * g->mz;
+  g->Next = 2 * g->M;
+  g->Nf = 4 * g->N + 4 * g->Next;
+  g->Ntot = g->Nf + 1;
+  g->lx = p->lx;
+  g->ly = p->ly;
+  g->lz = p->lz;
+  g->kxu = kTwoPi / p->lx;
+  g->kyu = kTwoPi / p->ly;
+  g->kzu = kTwoPi / p->lz;
+  g->kx2 = kTwoPi * kTwoPi / (p->lx * p->lx);
+  g->ky2 = kTwoPi * kTwoPi / (p->ly * p->ly);
+  g->kz2 = kTwoPi * kTwoPi / (p->lz * p->lz);
+  const double k2max = g->kx2 * (p->nx / 2) * (p->nx / 2) + g->ky2 * (p->ny / 2) * (p->ny / 2) +
+                       g->kz2 * (p->nz / 2) * (p->nz / 2);
+  g->kmax = sqrt(k2max);
+  g->kxmax = (p->nx / 2) * g->kxu;
+  g->kymax = (p->ny / 2) * g->kyu;
+  g->kzmax = (p->nz / 2) * g->kzu;
+  g->mass = p->mass;
+  g->bins = p->bins;
+}
+
+static int dmalloc(Ctx *c, void **p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    c->err = std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e);
+    return IH_ERR_ALLOC;
+  }
+  c->dev_bytes += bytes;
+  return IH_OK;
+}
+
+static int alloc_vec(Ctx *c, Vec &v) {
+  IH_TRY(dmalloc(c, &v.fl, c->tsize * c->g.Nf));
+  IH_CUDA(c, cudaMemsetAsync(v.fl, 0, c->tsize * c->g.Nf, c->stream));
+  IH_TRY(dmalloc(c, (void **)&v.sc, sizeof(double) * kSc));
+  IH_CUDA(c, cudaMemsetAsync(v.sc, 0, sizeof(double) * kSc, c->stream));
+  return IH_OK;
+}
+
+static void free_vec(Vec &v) {
+  if (v.fl) cudaFree(v.fl);
+  if (v.sc) cudaFree(v.sc);
+  v.fl = nullptr;
+  v.sc = nullptr;
+}
+
+static int create(const ih_params *p, Ctx *c) {
+  c->p = *p;
+  make_geom(p, &c->g);
+  c->mixed = p->precision == IH_PREC_MIXED;
+  c->tsize = c->mixed ? 4 : 8;
+  c->noise_eta = c->mixed ? kDefaultNoiseEta : 0.0;
+  IH_CUDA(c, cudaSetDevice(p->device));
+  IH_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  const Geom &g = c->g;
+  const size_t cs = 2 * c->tsize;  // complex element
+  IH_TRY(fft_tables(c));
+  void *specblk = nullptr;
+  IH_TRY(dmalloc(c, &specblk, cs * (size_t)g.M * 7));
+  for (int i = 0; i < 7; ++i) c->spec[i] = (char *)specblk + cs * (size_t)g.M * i;
+  void *rblk = nullptr;
+  IH_TRY(dmalloc(c, &rblk, c->tsize * (size_t)g.N * 4));
+  for (int i = 0; i < 4; ++i) c->rbuf[i] = (char *)rblk + c->tsize * (size_t)g.N * i;
+  IH_TRY(dmalloc(c, &c->mask, c->tsize * (size_t)g.M));
+  // FP64 partial sums: the fused RHS pass writes 2 per tile of rows
+  c->partials_cap = (long long)kMaxPartials * 8;
+  if (2LL * g.nx * g.ny + 64 > c->partials_cap) c->partials_cap = 2LL * g.nx * g.ny + 64;
+  IH_TRY(dmalloc(c, (void **)&c->partials, sizeof(double) * (size_t)c->partials_cap));
+  IH_TRY(dmalloc(c, (void **)&c->rs, sizeof(RhsScalars)));
+  IH_CUDA(c, cudaMemsetAsync(c->rs, 0, sizeof(RhsScalars), c->stream));
+  IH_TRY(dmalloc(c, (void **)&c->diag, sizeof(double) * (4 * g.bins + 128)));
+  IH_CUDA(c, cudaMemsetAsync(c->diag, 0, sizeof(double) * (4 * g.bins + 128), c->stream));
+  c->hpin_bytes = 4096;
+  IH_CUDA(c, cudaMallocHost((void **)&c->hpin, c->hpin_bytes));
+  IH_TRY(dmalloc(c, &c->stage_dev, sizeof(double) * (size_t)g.Ntot));
+  IH_TRY(alloc_vec(c, c->y));
+  IH_TRY(alloc_vec(c, c->ynew));
+  IH_TRY(alloc_vec(c, c->ytmp));
+  IH_TRY(alloc_vec(c, c->k[1]));
+  IH_TRY(mask_init(c, c->mask));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
+static void destroy(Ctx *c) {
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->tw_x) cudaFree(c->tw_x);
+  if (c->tw_y) cudaFree(c->tw_y);
+  if (c->tw_h) cudaFree(c->tw_h);
+  if (c->tw_z) cudaFree(c->tw_z);
+  if (c->spec[0]) cudaFree(c->spec[0]);
+  if (c->rbuf[0]) cudaFree(c->rbuf[0]);
+  if (c->mask) cudaFree(c->mask);
+  if (c->partials) cudaFree(c->partials);
+  if (c->rs) cudaFree(c->rs);
+  if (c->diag) cudaFree(c->diag);
+  if (c->hpin) cudaFreeHost(c->hpin);
+  if (c->stage_dev) cudaFree(c->stage_dev);
+  free_vec(c->y);
+  free_vec(c->ynew);
+  free_vec(c->ytmp);
+  for (int j = 0; j < 13; ++j) free_vec(c->k[j]);
+  for (auto &t : c->timers)
+    for (auto e : t.ev) cudaEventDestroy(e);
+  for (auto e : c->tev)
+    if (e) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+static int upload_ref(Ctx *c, const double *host) {
+  IH_CUDA(c, cudaMemcpyAsync(c->stage_dev, host, sizeof(double) * c->g.Ntot,
+                             cudaMemcpyHostToDevice, c->stream));
+  return IH_OK;
+}
+static int download_ref(Ctx *c, double *host) {
+  IH_CUDA(c, cudaMemcpyAsync(host, c->stage_dev, sizeof(double) * c->g.Ntot,
+                             cudaMemcpyDeviceToHost, c->stream));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
+}  // namespace ih
+
+using namespace ih;
+
+struct ih_context {
+  Ctx c;
+};
+
+#define CTX_CHECK(ctx)           \
+  do {                           \
+    if (!(ctx)) return IH_ERR_ARG; \
+  } while (0)
+
+extern "C" {
+
+const char *ih_status_string(int s) {
+  switch (s) {
+    case IH_OK: return "ok";
+    case IH_ERR_ARG: return "invalid argument";
+    case IH_ERR_CUDA: return "CUDA error";
+    case IH_ERR_ALLOC: return "allocation failed";
+    case IH_ERR_STATE: return "call out of order";
+    case IH_ERR_UNDERFLOW: return "step size underflow";
+    case IH_ERR_NAN: return "non-finite value";
+    default: return "unknown status";
+  }
+}
+
+int ih_sizes(int nx, int ny, int nz, size_t *N, size_t *M, size_t *Next, size_t *Ntot) {
+  if (nx < 1 || ny < 1 || nz < 2) return IH_ERR_ARG;
+  size_t n = (size_t)nx * ny * nz, m = (size_t)nx * ny * (nz / 2 + 1);
+  if (N) *N = n;
+  if (M) *M = m;
+  if (Next) *Next = 2 * m;
+  if (Ntot) *Ntot = 4 * n + 4 * 2 * m + 1;
+  return IH_OK;
+}
+
+int ih_create(const ih_params *p, ih_context **out) {
+  if (!out) return IH_ERR_ARG;
+  *out = nullptr;
+  std::string why;
+  int s = validate(p, &why);
+  if (s != IH_OK) return s;
+  ih_context *h = new (std::nothrow) ih_context();
+  if (!h) return IH_ERR_ALLOC;
+  s = create(p, &h->c);
+  if (s != IH_OK) {
+    destroy(&h->c);
+    delete h;
+    return s;
+  }
+  *out = h;
+  return IH_OK;
+}
+
+void ih_destroy(ih_context *h) {
+  if (!h) return;
+  destroy(&h->c);
+  delete h;
+}
+
+const char *ih_last_error(const ih_context *h) { return h ? h->c.err.c_str() : "null context"; }
+size_t ih_device_bytes(const ih_context *h) { return h ? h->c.dev_bytes : 0; }
+double ih_time(const ih_context *h) { return h ? h->c.t : 0.0; }
+unsigned long long ih_calls_rhs(const ih_context *h) { return h ? h->c.calls_rhs : 0; }
+unsigned long long ih_kernel_launches(const ih_context *h) { return h ? h->c.launches : 0; }
+
+int ih_set_state(ih_context *h, const double *f, double t) {
+  CTX_CHECK(h);
+  if (!f) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  IH_TRY(upload_ref(c, f));
+  IH_TRY(vec_from_ref(c, (const double *)c->stage_dev, c->y));
+  c->t = t;
+  c->have_state = 1;
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
+int ih_get_state(ih_context *h, double *f) {
+  CTX_CHECK(h);
+  if (!f) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  IH_TRY(vec_to_ref(c, c->y, (double *)c->stage_dev));
+  return download_ref(c, f);
+}
+
+int ih_set_dstate(ih_context *h, const double *df) {
+  CTX_CHECK(h);
+  if (!df) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  IH_TRY(upload_ref(c, df));
+  IH_TRY(vec_from_ref(c, (const double *)c->stage_dev, c->k[1]));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
+int ih_get_dstate(ih_context *h, double *df) {
+  CTX_CHECK(h);
+  if (!df) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  IH_TRY(vec_to_ref(c, c->k[1], (double *)c->stage_dev));
+  return download_ref(c, df);
+}
+
+int ih_mk_rhs_dev(ih_context *h, double t, double *f_dev, double *result_dev, int filter,
+                  int output) {
+  CTX_CHECK(h);
+  if (!f_dev || !result_dev) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  IH_TRY(vec_from_ref(c, f_dev, c->ytmp));
+  IH_TRY(rhs(c, t, c->ytmp, c->ynew, filter, output, nullptr));
+  if (filter == 1 && c->p.enable_filter) IH_TRY(vec_to_ref(c, c->ytmp, f_dev));
+  const Geom &g = c->g;
+  if (c->p.enable_gw) {
+    IH_TRY(vec_to_ref(c, c->ynew, result_dev));
+  } else {
+    // the reference leaves the tensor part of result untouched without GW
+    IH_TRY(vec_to_ref(c, c->ynew, (double *)c->stage_dev));
+    IH_CUDA(c, cudaMemcpyAsync(result_dev, c->stage_dev, sizeof(double) * 4 * g.N,
+                               cudaMemcpyDeviceToDevice, c->stream));
+    IH_CUDA(c, cudaMemcpyAsync(result_dev + g.Nf, (double *)c->stage_dev + g.Nf, sizeof(double),
+                               cudaMemcpyDeviceToDevice, c->stream));
+  }
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
+int ih_mk_rhs_host(ih_context *h, double t, double *f, double *result, int filter, int output) {
+  CTX_CHECK(h);
+  if (!f || !result) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  const Geom &g = c->g;
+  IH_TRY(upload_ref(c, f));
+  IH_TRY(vec_from_ref(c, (const double *)c->stage_dev, c->ytmp));
+  IH_TRY(rhs(c, t, c->ytmp, c->ynew, filter, output, nullptr));
+  if (filter == 1 && c->p.enable_filter) {
+    IH_TRY(vec_to_ref(c, c->ytmp, (double *)c->stage_dev));
+    IH_TRY(download_ref(c, f));
+  }
+  IH_TRY(vec_to_ref(c, c->ynew, (double *)c->stage_dev));
+  if (c->p.enable_gw) return download_ref(c, result);
+  IH_CUDA(c, cudaMemcpyAsync(result, c->stage_dev, sizeof(double) * 4 * g.N,
+                             cudaMemcpyDeviceToHost, c->stream));
+  IH_CUDA(c, cudaMemcpyAsync(result + g.Nf, (double *)c->stage_dev + g.Nf, sizeof(double),
+                             cudaMemcpyDeviceToHost, c->stream));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
+int ih_get_means(const ih_context *hc, double *rho_mean, double *pressure_mean) {
+  if (!hc) return IH_ERR_ARG;
+  ih_context *h = const_cast<ih_context *>(hc);
+  Ctx *c = &h->c;
+  IH_CUDA(c, cudaMemcpyAsync(&c->rs_host, c->rs, sizeof(RhsScalars), cudaMemcpyDeviceToHost,
+                             c->stream));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (rho_mean) *rho_mean = c->rs_host.rho_mean;
+  if (pressure_mean) *pressure_mean = c->rs_host.p_mean;
+  return IH_OK;
+}
+
+int ih_get_field(ih_context *h, int which, double *out) {
+  CTX_CHECK(h);
+  if (!out) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  IH_TRY(get_field(c, which, (double *)c->stage_dev));
+  IH_CUDA(c, cudaMemcpyAsync(out, c->stage_dev, sizeof(double) * c->g.N, cudaMemcpyDeviceToHost,
+                             c->stream));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
+int ih_get_output(ih_context *h, ih_output *out) {
+  CTX_CHECK(h);
+  if (!out) return IH_ERR_ARG;
+  return read_output(&h->c, out);
+}
+
+int ih_fft_host(ih_context *h, const double *in, double *out_c) {
+  CTX_CHECK(h);
+  if (!in || !out_c) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  const Geom &g = c->g;
+  double *din = (double *)c->stage_dev, *dout = din + g.N;
+  IH_CUDA(c, cudaMemcpyAsync(din, in, sizeof(double) * g.N, cudaMemcpyHostToDevice, c->stream));
+  IH_TRY(fft_any(c, din, dout));
+  IH_CUDA(c, cudaMemcpyAsync(out_c, dout, sizeof(double) * 2 * g.M, cudaMemcpyDeviceToHost,
+                             c->stream));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
+int ih_ifft_host(ih_context *h, const double *in_c, double *out) {
+  CTX_CHECK(h);
+  if (!in_c || !out) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  const Geom &g = c->g;
+  double *din = (double *)c->stage_dev, *dout = din + 2 * g.M;
+  IH_CUDA(c, cudaMemcpyAsync(din, in_c, sizeof(double) * 2 * g.M, cudaMemcpyHostToDevice,
+                             c->stream));
+  IH_TRY(ifft_any(c, din, dout));
+  IH_CUDA(c, cudaMemcpyAsync(out, dout, sizeof(double) * g.N, cudaMemcpyDeviceToHost,
+                             c->stream));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
+int ih_ic_fluctuations(ih_context *h, uint64_t seed, double phi0, double dphi0, double a0,
+                       double amp, double kcut) {
+  CTX_CHECK(h);
+  Ctx *c = &h->c;
+  IH_TRY(ic_fluctuations(c, seed, phi0, dphi0, a0, amp, kcut));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_state = 1;
+  c->dopri_ready = 0;
+  return IH_OK;
+}
+
+int ih_initial_psi(ih_context *h) {
+  CTX_CHECK(h);
+  Ctx *c = &h->c;
+  if (!c->have_state) {
+    c->err = "no state";
+    return IH_ERR_STATE;
+  }
+  IH_TRY(initial_psi(c));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->dopri_ready = 0;
+  return IH_OK;
+}
+
+int ih_dopri853_init(ih_context *h, const ih_dopri_cfg *cfg, double t0, double dt0) {
+  CTX_CHECK(h);
+  if (!cfg || !(cfg->rtol >= 0) || !(cfg->atol >= 0) || !(dt0 > 0)) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  if (!c->have_state) {
+    c->err = "no state";
+    return IH_ERR_STATE;
+  }
+  IH_TRY(dopri_init(c, cfg, t0, dt0));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
+int ih_dopri853_step(ih_context *h, double dt_try, int want_output, ih_step_info *info) {
+  CTX_CHECK(h);
+  if (!(dt_try > 0)) return IH_ERR_ARG;
+  return dopri_step(&h->c, dt_try, want_output, info);
+}
+
+int ih_dopri853_run(ih_context *h, double tf, long max_steps, double *log, long log_cap,
+                    long *n_steps) {
+  CTX_CHECK(h);
+  Ctx *c = &h->c;
+  if (!c->dopri_ready) {
+    c->err = "ih_dopri853_init has not been called";
+    return IH_ERR_STATE;
+  }
+  // the run loop of dopri853.c:118-155 (I/O and wall-clock limits are the
+  // caller's; the C99 drop-in layer adds them)
+  double dt = c->dt_next;
+  long accepted = 0;
+  int status = IH_OK;
+  for (c->n_stp = 0;; ++c->n_stp) {
+    if (c->t + dt * 1.0001 > tf) dt = tf - c->t;
+    ih_step_info info;
+    status = dopri_step(c, dt, 0, &info);
+    if (status != IH_OK) break;
+    ++accepted;
+    if (info.dt_did == dt) ++c->n_ok;
+    else ++c->n_bad;
+    if (log && c->n_stp < log_cap) {
+      log[4 * c->n_stp] = info.t;
+      log[4 * c->n_stp + 1] = info.dt_did;
+      log[4 * c->n_stp + 2] = info.err;
+      log[4 * c->n_stp + 3] = info.tries;
+    }
+    if (c->t >= tf) break;
+    if (c->n_stp + 1 >= max_steps) break;
+    if (fabs(c->dt_next) <= c->cfg.dt_min) break;
+    dt = c->dt_next;
+  }
+  if (n_steps) *n_steps = accepted;
+  return status;
+}
+
+int ih_dopri853_counters(const ih_context *h, double *dt_next, long *n_ok, long *n_bad,
+                         long *n_tries) {
+  if (!h) return IH_ERR_ARG;
+  const Ctx *c = &h->c;
+  if (dt_next) *dt_next = c->dt_next;
+  if (n_ok) *n_ok = c->n_ok;
+  if (n_bad) *n_bad = c->n_bad;
+  if (n_tries) *n_tries = c->n_tries;
+  return IH_OK;
+}
+
+int ih_dopri853_tableau(double *cc, double *a, double *b, double *bhh, double *er) {
+  dopri_tableau(cc, a, b, bhh, er);
+  return IH_OK;
+}
+
+int ih_rk4_step(ih_context *h, double dt, int want_output) {
+  CTX_CHECK(h);
+  Ctx *c = &h->c;
+  if (!c->have_state) {
+    c->err = "no state";
+    return IH_ERR_STATE;
+  }
+  IH_TRY(rk4_step(c, dt, want_output));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
+int ih_sync(ih_context *h) {
+  CTX_CHECK(h);
+  Ctx *c = &h->c;
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
+int ih_profile_enable(ih_context *h, int on) {
+  CTX_CHECK(h);
+  Ctx *c = &h->c;
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (auto &t : c->timers) {
+    for (auto e : t.ev) cudaEventDestroy(e);
+    t.ev.clear();
+    t.bytes = 0.0;
+    t.launches = 0;
+  }
+  c->prof_on = on;
+  return IH_OK;
+}
+
+static double timer_ms(Timer &t) {
+  double total = 0.0;
+  for (size_t i = 0; i + 1 < t.ev.size(); i += 2) {
+    float f = 0.f;
+    cudaEventElapsedTime(&f, t.ev[i], t.ev[i + 1]);
+    total += f;
+  }
+  return total;
+}
+
+int ih_profile_read(ih_context *h, int cls, double *ms, long *launches) {
+  CTX_CHECK(h);
+  if (cls < 0 || cls > 2) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  double total = 0.0;
+  long n = 0;
+  for (int k = 0; k < KK_COUNT; ++k) {
+    if (kernel_kind_class(k) != cls) continue;
+    total += timer_ms(c->timers[k]);
+    n += c->timers[k].launches;
+  }
+  if (ms) *ms = total;
+  if (launches) *launches = n;
+  return IH_OK;
+}
+
+int ih_profile_kernel(ih_context *h, int kind, double *ms, long *launches, double *bytes) {
+  CTX_CHECK(h);
+  if (kind < 0 || kind >= KK_COUNT) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  Timer &t = c->timers[kind];
+  if (ms) *ms = timer_ms(t);
+  if (launches) *launches = t.launches;
+  if (bytes) *bytes = t.bytes;
+  return IH_OK;
+}
+
+const char *ih_profile_kernel_name(int kind) { return kernel_kind_name(kind); }
+int ih_profile_kernel_count(void) { return KK_COUNT; }
+
+int ih_timer_start(ih_context *h) {
+  CTX_CHECK(h);
+  Ctx *c = &h->c;
+  for (int i = 0; i < 2; ++i)
+    if (!c->tev[i]) IH_CUDA(c, cudaEventCreate(&c->tev[i]));
+  IH_CUDA(c, cudaEventRecord(c->tev[0], c->stream));
+  return IH_OK;
+}
+
+int ih_timer_stop(ih_context *h, double *ms) {
+  CTX_CHECK(h);
+  Ctx *c = &h->c;
+  if (!c->tev[0]) return IH_ERR_STATE;
+  IH_CUDA(c, cudaEventRecord(c->tev[1], c->stream));
+  IH_CUDA(c, cudaEventSynchronize(c->tev[1]));
+  float f = 0.f;
+  IH_CUDA(c, cudaEventElapsedTime(&f, c->tev[0], c->tev[1]));
+  if (ms) *ms = f;
+  return IH_OK;
+}
+
+int ih_host_alloc(size_t bytes, void **out) {
+  if (!out) return IH_ERR_ARG;
+  *out = nullptr;
+  if (cudaMallocHost(out, bytes) != cudaSuccess) return IH_ERR_ALLOC;
+  return IH_OK;
+}
+
+int ih_host_free(void *p) {
+  if (p && cudaFreeHost(p) != cudaSuccess) return IH_ERR_CUDA;
+  return IH_OK;
+}
+
+int ih_dopri853_set_noise_floor(ih_context *h, double eta) {
+  CTX_CHECK(h);
+  if (!(eta >= 0.0)) return IH_ERR_ARG;
+  h->c.noise_eta = eta;
+  return IH_OK;
+}
+
+}  // extern "C"

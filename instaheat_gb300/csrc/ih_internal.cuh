@@ -1,0 +1,235 @@
+// ih_internal.cuh -- private types and cross-file declarations of
+// libinstaheat_gpu.so (GB300, sm_103a).
+//
+// Device data layout
+// ------------------
+// A state vector (the reference's `field`, `dfield`, the DOPRI853 stage
+// vectors k2..k12, k_tmp, field_new) is split into
+//   fl : T[Nf], Nf = 4N + 4Next, segments phi, dphi, psi, dpsi (N each, real
+//        space, [x][y][z]) then h1, h2, dh1, dh2 (Next each, interleaved
+//        complex half spectrum [x][y][z/2+1]) -- the reference order without a;
+//   sc : double[8], sc[0..3] the homogeneous (k = 0) parts of phi, dphi, psi,
+//        dpsi and sc[4] the scale factor a.
+// The value of component i of segment s < 4 is sc[s] + fl[i]; h and a are
+// fl and sc[4] alone.  In the plain FP64 form T = double and sc[0..3] stay 0,
+// so fl is exactly the reference's array.  In the mixed form T = float and
+// the homogeneous parts live in FP64; the filter pass moves the k = 0 mode of
+// fl into sc once per accepted step.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include <string>
+#include <vector>
+#include "../../include/instaheat_gpu.h"
+
+namespace ih {
+
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+constexpr double kPi = 3.141592653589793238462643383279;
+constexpr int kSc = 8;          // doubles of FP64 scalars per vector
+constexpr int kMaxPartials = 4096;
+// Mixed form: each FP32 error-vector element is soft-thresholded by
+// eta * eps32 * sum_j |c_j k_j| before it enters the FP64 error norm.
+constexpr double kDefaultNoiseEta = 32.0;
+
+template <typename T> struct Cplx;
+template <> struct Cplx<float> { using type = float2; };
+template <> struct Cplx<double> { using type = double2; };
+template <typename T> using C2 = typename Cplx<T>::type;
+
+// Grid geometry shared by host and device code.
+struct Geom {
+  int nx, ny, nz, h, mz;        // h = nz/2 (complex z length), mz = nz/2 + 1
+  long long N, M, Next, Nf, Ntot;
+  double lx, ly, lz;
+  double kxu, kyu, kzu;         // 2 pi / L per axis (pars.x.k)
+  double kx2, ky2, kz2;         // (2 pi / L)^2 per axis (pars.x.k2)
+  double kmax;                  // sqrt(k2_max), setup.c:661-664
+  double kxmax, kymax, kzmax;   // filter denominators, setup.c:712-714
+  double mass;
+  int bins;
+};
+
+// RHS scalars produced on the device by the reduction-finish kernel.
+struct RhsScalars {
+  double rho_mean, p_mean;      // <rho>, <p> (full values)
+  double H, a, a2;              // sqrt(<rho>/3), a, a^2
+  double rho_bar, p_bar;        // FP64 homogeneous parts (mixed form)
+  double dphi_mean, phi_mean;   // full means (psi solve, constraints)
+  double ddphi_mean;            // mean of the dphi-RHS (psi solve)
+  int nonfinite;                // set when a reduction saw NaN/Inf
+  int pad;
+};
+
+struct Vec {                    // one state-shaped vector
+  void *fl = nullptr;           // T[Nf]
+  double *sc = nullptr;         // double[kSc] (device)
+};
+
+// kernel kinds for per-kernel timing and algorithmic-byte accounting
+enum KernelKind {
+  KK_FFT_XY = 0,        // complex pass along x or y
+  KK_FFT_ZR2C,          // real-to-complex pass along z
+  KK_FFT_ZC2R,          // complex-to-real pass along z
+  KK_X_DERIV4,          // inverse x pass generating the 4 derivative spectra
+  KK_Z_RHS_FUSED,       // last inverse z pass + pointwise + GW products
+  KK_UPDATE_H,          // TT projection + tensor equation of motion
+  KK_UPDATE_PHI_PSI,    // phi/psi equations of motion
+  KK_FILTER,            // spectral filter
+  KK_LINCOMB,           // DOPRI853/RK4 stage combination
+  KK_DOPRI_FINAL,       // field_new + embedded error sums
+  KK_COUNT
+};
+const char *kernel_kind_name(int k);
+int kernel_kind_class(int k);     // 0 FFT, 1 pointwise, 2 stepper
+
+struct Timer {                  // per-kind CUDA-event accumulation
+  std::vector<cudaEvent_t> ev;  // pairs
+  long launches = 0;
+  double bytes = 0.0;           // algorithmic bytes of the timed launches
+};
+
+struct Ctx {
+  ih_params p{};
+  Geom g{};
+  int mixed = 0;                // IH_PREC_MIXED
+  size_t tsize = 8;             // sizeof(T)
+  cudaStream_t stream = nullptr;
+  std::string err;
+  size_t dev_bytes = 0;
+  unsigned long long calls_rhs = 0;
+  unsigned long long launches = 0;
+
+  // FFT tables (T complex): exp(-2 pi i k / L) for L = nx, ny, h and nz.
+  void *tw_x = nullptr, *tw_y = nullptr, *tw_h = nullptr, *tw_z = nullptr;
+
+  // RHS temporaries
+  void *spec[7] = {};           // complex M each (T)
+  void *rbuf[4] = {};           // real N each: 0 lap, 1 p (fluct), 2 rho (fluct), 3 lap psi
+  void *mask = nullptr;         // filter mask, M values of T
+  double *partials = nullptr;   // partials_cap doubles
+  long long partials_cap = 0;
+  RhsScalars *rs = nullptr;     // device
+  RhsScalars rs_host{};
+  double *diag = nullptr;       // device: 4 spectra * bins + 4 cstr + 24 smry + misc
+  double *hpin = nullptr;       // pinned host staging: small values
+  size_t hpin_bytes = 0;
+
+  // state and stepper vectors
+  Vec y, ynew, ytmp, k[13];     // k[1..12] stage RHS, k[1] = dfield
+  double t = 0.0;
+  int have_state = 0, dopri_ready = 0;
+  ih_dopri_cfg cfg{};
+  double dt_next = 0.0, err_old = 1.0e-4;
+  int reject = 0;
+  long n_ok = 0, n_bad = 0, n_stp = 0, n_tries = 0;
+  double last_err = 0.0;
+
+  // host staging for transfers
+  void *stage_dev = nullptr;    // FP64 device buffer of Ntot (reference layout)
+
+  // profiling
+  int prof_on = 0;
+  Timer timers[KK_COUNT];
+  cudaEvent_t tev[2] = {nullptr, nullptr};  // ih_timer_start/stop
+  double noise_eta = 0.0;       // FP32 rounding floor factor of the error norm
+
+  // last output flag results available
+  int have_output = 0;
+};
+
+// ---------------------------------------------------------------------------
+// error helpers
+#define IH_CUDA(ctx, call)                                                   \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess) {                                                 \
+      (ctx)->err = std::string(#call) + ": " + cudaGetErrorString(e_);       \
+      return IH_ERR_CUDA;                                                    \
+    }                                                                        \
+  } while (0)
+
+#define IH_TRY(expr)                                                         \
+  do {                                                                       \
+    int s_ = (expr);                                                         \
+    if (s_ != IH_OK) return s_;                                              \
+  } while (0)
+
+int check_launch(Ctx *c, const char *what);
+
+// profiling brackets around one launch of kernel kind `kind`; `bytes` are
+// the launch's algorithmic bytes (each input read once, each output written once)
+void prof_begin(Ctx *c, int kind);
+void prof_end(Ctx *c, int kind, double bytes);
+
+// ---------------------------------------------------------------------------
+// FFT (ih_fft.cu).  All transforms are batched over `count` arrays that are
+// `stride` elements apart.  Complex arrays: M = nx*ny*mz elements of C2<T>.
+template <typename T>
+int fft_r2c(Ctx *c, const T *in, long long in_stride, C2<T> *out,
+            long long out_stride, int count);
+template <typename T>
+int fft_c2r(Ctx *c, C2<T> *in_destroyed, long long in_stride, T *out,
+            long long out_stride, int count);
+// The three passes, exposed for fused pipelines.
+template <typename T>
+int fft_zr2c(Ctx *c, const T *in, long long in_stride, C2<T> *out,
+             long long out_stride, int count);
+template <typename T>
+int fft_zc2r(Ctx *c, const C2<T> *in, long long in_stride, T *out,
+             long long out_stride, int count);
+// axis 0 = x, 1 = y; sign -1 forward, +1 backward; in place.
+template <typename T>
+int fft_xy(Ctx *c, C2<T> *data, long long stride, int count, int axis,
+           int sign);
+// Inverse x-pass that generates the four derivative spectra from phi-hat:
+// out[a] = F_a(k) * phihat(k) / N, a = d/dx, d/dy, d/dz, laplacian, then the
+// inverse x transform of each; phihat is only read.
+template <typename T>
+int fft_x_deriv4_inv(Ctx *c, const C2<T> *phihat, C2<T> *out,
+                     long long out_stride);
+// Fused last inverse z pass for the RHS: c2r of the four derivative spectra,
+// then per point (grad phi)^2, rho, p (and their FP64 block sums), writes the
+// laplacian and p (and rho), and when gw the six products d_i phi d_j phi
+// transformed forward along z into six half spectra.
+template <typename T>
+int fft_z_rhs_fused(Ctx *c, const C2<T> *d4, const T *yfl, const double *ysc,
+                    T *lap, T *p, T *rho, C2<T> *s6, int gw, double *partials,
+                    int *nblocks_out);
+
+int fft_tables(Ctx *c);
+
+// ---------------------------------------------------------------------------
+// RHS and helpers (ih_rhs.cu)
+int rhs(Ctx *c, double t, Vec &y, Vec &k, int filter, int output,
+        const Vec *smry_src);
+int reduce_mean(Ctx *c, const void *arr, long long n, double *dev_out);
+int ic_fluctuations(Ctx *c, uint64_t seed, double phi0, double dphi0,
+                    double a0, double amp, double kcut);
+int initial_psi(Ctx *c);
+int vec_from_ref(Ctx *c, const double *ref_dev, Vec &v);
+int vec_to_ref(Ctx *c, const Vec &v, double *ref_dev);
+int vec_copy(Ctx *c, const Vec &src, Vec &dst);
+int ifft_any(Ctx *c, const double *in_c_dev, double *out_dev);
+int fft_any(Ctx *c, const double *in_dev, double *out_c_dev);
+int get_field(Ctx *c, int which, double *dev_out);
+int read_output(Ctx *c, ih_output *out);
+int mask_init(Ctx *c, void *mask);
+int convert_add(Ctx *c, const void *a, double add, long long n, double *out);
+
+// stepper (ih_stepper.cu)
+int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0);
+int dopri_step(Ctx *c, double dt_try, int want_output, ih_step_info *info);
+int rk4_step(Ctx *c, double dt, int want_output);
+void dopri_tableau(double *cc, double *a, double *b, double *bhh, double *er);
+
+// launch geometry helper: blocks for n items with `per` items per thread
+inline unsigned grid_for(long long n, int threads, int per = 1) {
+  long long b = (n + (long long)threads * per - 1) / ((long long)threads * per);
+  if (b < 1) b = 1;
+  if (b > 152LL * 16) b = 152LL * 16;  // grid-stride beyond 16 CTAs per SM
+  return (unsigned)b;
+}
+
+}  // namespace ih

@@ -1,0 +1,602 @@
+// ih_stepper.cu -- DOPRI853 (src/dopri853.c) and RK4 (src/rk4.c) on GB300.
+//
+// The state and all stage vectors stay on the device.  Per try the host
+// launches 11 stage combinations + 11 RHS evaluations and one fused kernel
+// that forms field_new and both embedded error sums (dopri853.c:438-486),
+// then reads back 4 doubles (error sums, <rho>, NaN flag) and runs the
+// reference's controller (dopri853.c:505-540) on the host.  Accepted steps
+// swap buffer pointers instead of copying field_new/dfield_new
+// (dopri853.c:301-305).
+//
+// Stage combinations and the final combination are bandwidth kernels over
+// Nf = 4N + 4Next elements: 16-byte vector loads (float4 / double2), grid
+// sized to a multiple of the 152 SMs, FP64 homogeneous parts handled by one
+// thread.
+#include <float.h>
+#include <math.h>
+#include <string.h>
+#include "ih_internal.cuh"
+
+namespace ih {
+
+// ---------------------------------------------------------------------------
+// Dormand-Prince 8(5,3) coefficients as published by Hairer, Norsett and
+// Wanner (code DOP853); the reference takes the same numbers from Numerical
+// Recipes (src/dopri853_constants.c).  Stages 1..12; A[i][j] = a_{i+1,j+1}.
+static double DA[12][12], DB[12], DE3[12], DBHH[3];
+static const double DC[12] = {0.0,
+                              0.526001519587677318785587544488e-01,
+                              0.789002279381515978178381316732e-01,
+                              0.118350341907227396726757197510e+00,
+                              0.281649658092772603273242802490e+00,
+                              0.333333333333333333333333333333e+00,
+                              0.25e+00,
+                              0.307692307692307692307692307692e+00,
+                              0.651282051282051282051282051282e+00,
+                              0.6e+00,
+                              0.857142857142857142857142857142e+00,
+                              1.0};
+static int tableau_ready = 0;
+
+static void tableau_init() {
+  if (tableau_ready) return;
+  memset(DA, 0, sizeof DA);
+  memset(DB, 0, sizeof DB);
+  memset(DE3, 0, sizeof DE3);
+  double(*A)[12] = DA;
+  A[1][0] = 5.26001519587677318785587544488e-2;
+  A[2][0] = 1.97250569845378994544595329183e-2;
+  A[2][1] = 5.91751709536136983633785987549e-2;
+  A[3][0] = 2.95875854768068491816892993775e-2;
+  A[3][2] = 8.87627564304205475450678981324e-2;
+  A[4][0] = 2.41365134159266685502369798665e-1;
+  A[4][2] = -8.84549479328286085344864962717e-1;
+  A[4][3] = 9.24834003261792003115737966543e-1;
+  A[5][0] = 3.7037037037037037037037037037e-2;
+  A[5][3] = 1.70828608729473871279604482173e-1;
+  A[5][4] = 1.25467687566822425016691814123e-1;
+  A[6][0] = 3.7109375e-2;
+  A[6][3] = 1.70252211019544039314978060272e-1;
+  A[6][4] = 6.02165389804559606850219397283e-2;
+  A[6][5] = -1.7578125e-2;
+  A[7][0] = 3.70920001185047927108779319836e-2;
+  A[7][3] = 1.70383925712239993810214054705e-1;
+  A[7][4] = 1.07262030446373284651809199168e-1;
+  A[7][5] = -1.53194377486244017527936158236e-2;
+  A[7][6] = 8.27378916381402288758473766002e-3;
+  A[8][0] = 6.24110958716075717114429577812e-1;
+  A[8][3] = -3.36089262944694129406857109825e0;
+  A[8][4] = -8.68219346841726006818189891453e-1;
+  A[8][5] = 2.75920996994467083049415600797e1;
+  A[8][6] = 2.01540675504778934086186788979e1;
+  A[8][7] = -4.34898841810699588477366255144e1;
+  A[9][0] = 4.77662536438264365890433908527e-1;
+  A[9][3] = -2.48811461997166764192642586468e0;
+  A[9][4] = -5.90290826836842996371446475743e-1;
+  A[9][5] = 2.12300514481811942347288949897e1;
+  A[9][6] = 1.52792336328824235832596922938e1;
+  A[9][7] = -3.32882109689848629194453265587e1;
+  A[9][8] = -2.03312017085086261358222928593e-2;
+  A[10][0] = -9.3714243008598732571704021658e-1;
+  A[10][3] = 5.18637242884406370830023853209e0;
+  A[10][4] = 1.09143734899672957818500254654e0;
+  A[10][5] = -8.14978701074692612513997267357e0;
+  A[10][6] = -1.85200656599969598641566180701e1;
+  A[10][7] = 2.27394870993505042818970056734e1;
+  A[10][8] = 2.49360555267965238987089396762e0;
+  A[10][9] = -3.0467644718982195003823669022e0;
+  A[11][0] = 2.27331014751653820792359768449e0;
+  A[11][3] = -1.05344954667372501984066689879e1;
+  A[11][4] = -2.00087205822486249909675718444e0;
+  A[11][5] = -1.79589318631187989172765950534e1;
+  A[11][6] = 2.79488845294199600508499808837e1;
+  A[11][7] = -2.85899827713502369474065508674e0;
+  A[11][8] = -8.87285693353062954433549289258e0;
+  A[11][9] = 1.23605671757943030647266201528e1;
+  A[11][10] = 6.43392746015763530355970484046e-1;
+  DB[0] = 5.42937341165687622380535766363e-2;
+  DB[5] = 4.45031289275240888144113950566e0;
+  DB[6] = 1.89151789931450038304281599044e0;
+  DB[7] = -5.8012039600105847814672114227e0;
+  DB[8] = 3.1116436695781989440891606237e-1;
+  DB[9] = -1.52160949662516078556178806805e-1;
+  DB[10] = 2.01365400804030348374776537501e-1;
+  DB[11] = 4.47106157277725905176885569043e-2;
+  DBHH[0] = 0.244094488188976377952755905512e+00;
+  DBHH[1] = 0.733846688281611857341361741547e+00;
+  DBHH[2] = 0.220588235294117647058823529412e-01;
+  DE3[0] = 0.1312004499419488073250102996e-01;
+  DE3[5] = -0.1225156446376204440720569753e+01;
+  DE3[6] = -0.4957589496572501915214079952e+00;
+  DE3[7] = 0.1664377182454986536961530415e+01;
+  DE3[8] = -0.3503288487499736816886487290e+00;
+  DE3[9] = 0.3341791187130174790297318841e+00;
+  DE3[10] = 0.8192320648511571246570742613e-01;
+  DE3[11] = -0.2235530786388629525884427845e-01;
+  tableau_ready = 1;
+}
+
+void dopri_tableau(double *cc, double *a, double *b, double *bhh, double *er) {
+  tableau_init();
+  if (cc) memcpy(cc, DC, sizeof DC);
+  if (a) memcpy(a, DA, sizeof DA);
+  if (b) memcpy(b, DB, sizeof DB);
+  if (bhh) memcpy(bhh, DBHH, sizeof DBHH);
+  if (er) memcpy(er, DE3, sizeof DE3);
+}
+
+// ---------------------------------------------------------------------------
+constexpr int kMaxTerms = 12;
+struct LinArgs {
+  const void *in[kMaxTerms];
+  const double *insc[kMaxTerms];
+  double coef[kMaxTerms];
+  int n;
+  double scale;  // out = base + scale * sum coef_j in_j
+};
+
+template <typename T> struct Vec4;
+template <> struct Vec4<float> {
+  using type = float4;
+  static constexpr int W = 4;
+};
+template <> struct Vec4<double> {
+  using type = double2;
+  static constexpr int W = 2;
+};
+
+template <typename T>
+__device__ __forceinline__ void vload(const T *p, T *v) {
+  if constexpr (sizeof(T) == 4) {
+    float4 q = *reinterpret_cast<const float4 *>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+  } else {
+    double2 q = *reinterpret_cast<const double2 *>(p);
+    v[0] = q.x; v[1] = q.y;
+  }
+}
+template <typename T>
+__device__ __forceinline__ void vstore(T *p, const T *v) {
+  if constexpr (sizeof(T) == 4) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  } else {
+    *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+  }
+}
+
+// y_stage = y + dt * sum_j a_sj k_j (dopri853.c:340-436, rk4.c:131-150)
+template <typename T>
+__global__ void k_lincomb(const T *__restrict__ base, const double *basesc, T *__restrict__ out,
+                          double *outsc, LinArgs args, long long nf) {
+  constexpr int W = Vec4<T>::W;
+  const long long nv = nf / W;
+  T cf[kMaxTerms];
+#pragma unroll
+  for (int j = 0; j < kMaxTerms; ++j) cf[j] = (T)args.coef[j];
+  const T sc = (T)args.scale;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
+       v += (long long)gridDim.x * blockDim.x) {
+    T acc[W], x[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) acc[w] = 0;
+#pragma unroll
+    for (int j = 0; j < kMaxTerms; ++j) {
+      if (j < args.n) {
+        vload<T>((const T *)args.in[j] + v * W, x);
+#pragma unroll
+        for (int w = 0; w < W; ++w) acc[w] += cf[j] * x[w];
+      }
+    }
+    vload<T>(base + v * W, x);
+#pragma unroll
+    for (int w = 0; w < W; ++w) x[w] = x[w] + sc * acc[w];
+    vstore<T>(out + v * W, x);
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 5) {
+    const int s = threadIdx.x;
+    double acc = 0.0;
+    for (int j = 0; j < args.n; ++j) acc += args.coef[j] * args.insc[j][s];
+    outsc[s] = basesc[s] + args.scale * acc;
+  }
+}
+
+// field_new and the two error sums of one DOPRI853 try (dopri853.c:438-486).
+// k[0..7] = stages 1, 6, 7, 8, 9, 10, 11, 12.
+struct FinalArgs {
+  const void *k[8];
+  const double *ksc[8];
+  double b[8], e5[8], e3[8];  // e5 = b - bhh on stages 1, 9, 12
+  double dt, rtol, atol;
+  double noise;               // eta * eps32 (mixed form), 0 for FP64
+};
+
+template <typename T>
+__global__ void k_dopri_final(const T *__restrict__ y, const double *ysc, T *__restrict__ ynew,
+                              double *ynsc, FinalArgs a, long long N, long long nf,
+                              double *partials) {
+  constexpr int W = Vec4<T>::W;
+  const long long nv = nf / W;
+  // homogeneous parts of the three combinations (every thread, FP64)
+  double sb[5], s5[5], s3[5], ysv[5], ynv[5];
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    double x = 0.0, e5 = 0.0, e3 = 0.0;
+    for (int j = 0; j < 8; ++j) {
+      const double kv = a.ksc[j][s];
+      x += a.b[j] * kv;
+      e5 += a.e5[j] * kv;
+      e3 += a.e3[j] * kv;
+    }
+    sb[s] = x;
+    s5[s] = e5;
+    s3[s] = e3;
+    ysv[s] = ysc[s];
+    ynv[s] = ysc[s] + a.dt * x;
+  }
+  T cb[8], c5[8], c3[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    cb[j] = (T)a.b[j];
+    c5[j] = (T)a.e5[j];
+    c3[j] = (T)a.e3[j];
+  }
+  const T dtT = (T)a.dt;
+  double err = 0.0, err2 = 0.0;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
+       v += (long long)gridDim.x * blockDim.x) {
+    T ab[W], a5[W], a3[W], t5[W], t3[W], x[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) ab[w] = a5[w] = a3[w] = t5[w] = t3[w] = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      vload<T>((const T *)a.k[j] + v * W, x);
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        ab[w] += cb[j] * x[w];
+        a5[w] += c5[j] * x[w];
+        a3[w] += c3[j] * x[w];
+        if constexpr (sizeof(T) == 4) {
+          t5[w] += fabsf(c5[j] * x[w]);
+          t3[w] += fabsf(c3[j] * x[w]);
+        }
+      }
+    }
+    T yv[W], yn[W];
+    vload<T>(y + v * W, yv);
+#pragma unroll
+    for (int w = 0; w < W; ++w) yn[w] = yv[w] + dtT * ab[w];
+    vstore<T>(ynew + v * W, yn);
+    const long long i0 = v * W;
+    const int seg = i0 < 4 * N ? (int)(i0 / N) : 4;  // W divides N: one segment per vector
+    if constexpr (sizeof(T) == 4) {
+      // mixed form: per-element arithmetic in FP32, FP32 rounding floor
+      // removed, sums of squares accumulated in FP64
+      const float nz = (float)a.noise;
+      const float ys = seg < 4 ? (float)ysv[seg] : 0.f, yns = seg < 4 ? (float)ynv[seg] : 0.f;
+      const float q5s = seg < 4 ? (float)s5[seg] : 0.f, q3s = seg < 4 ? (float)s3[seg] : 0.f;
+      float acc5 = 0.f, acc3 = 0.f;
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        float f5 = fmaxf(fabsf(a5[w]) - nz * t5[w], 0.f);
+        float f3 = fmaxf(fabsf(a3[w]) - nz * t3[w], 0.f);
+        float q5 = copysignf(f5, a5[w]) + q5s, q3 = copysignf(f3, a3[w]) + q3s;
+        float sk = (float)a.atol + (float)a.rtol * fmaxf(fabsf(ys + yv[w]), fabsf(yns + yn[w]));
+        float r5 = q5 / sk, r3 = q3 / sk;
+        acc5 += r5 * r5;
+        acc3 += r3 * r3;
+      }
+      err2 += (double)acc5;
+      err += (double)acc3;
+    } else {
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        double yf = (double)yv[w], ynf = (double)yn[w], q5 = (double)a5[w], q3 = (double)a3[w];
+        if (seg < 4) {
+          yf += ysv[seg];
+          ynf += ynv[seg];
+          q5 += s5[seg];
+          q3 += s3[seg];
+        }
+        const double sk = a.atol + a.rtol * fmax(fabs(yf), fabs(ynf));
+        const double r5 = q5 / sk, r3 = q3 / sk;
+        err2 += r5 * r5;
+        err += r3 * r3;
+      }
+    }
+  }
+  // scale factor a (the last state component)
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const double sk = a.atol + a.rtol * fmax(fabs(ysv[4]), fabs(ynv[4]));
+    const double r5 = s5[4] / sk, r3 = s3[4] / sk;
+    err2 += r5 * r5;
+    err += r3 * r3;
+#pragma unroll
+    for (int s = 0; s < 5; ++s) ynsc[s] = ynv[s];
+    ynsc[5] = ynsc[6] = ynsc[7] = 0.0;
+  }
+  // block reduction
+  for (int o = 16; o > 0; o >>= 1) {
+    err += __shfl_down_sync(0xffffffffu, err, o);
+    err2 += __shfl_down_sync(0xffffffffu, err2, o);
+  }
+  __shared__ double red[2][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][wid] = err;
+    red[1][wid] = err2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s0 = 0.0, s1 = 0.0;
+    for (int w = 0; w < (int)(blockDim.x / 32); ++w) {
+      s0 += red[0][w];
+      s1 += red[1][w];
+    }
+    partials[2 * blockIdx.x] = s0;
+    partials[2 * blockIdx.x + 1] = s1;
+  }
+}
+
+// error() (dopri853.c:469-486) -> out[0]; <rho> and the NaN flag of the last
+// RHS -> out[1], out[2]
+__global__ void k_dopri_err_finish(const double *partials, int nb, double dt, double ntot,
+                                   const RhsScalars *rs, double *out) {
+  double e = 0.0, e2 = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    e += partials[2 * b];
+    e2 += partials[2 * b + 1];
+  }
+  __shared__ double sh[2][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    e += __shfl_down_sync(0xffffffffu, e, o);
+    e2 += __shfl_down_sync(0xffffffffu, e2, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = e;
+    sh[1][threadIdx.x >> 5] = e2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double err = 0.0, err2 = 0.0;
+    for (int w = 0; w < (int)(blockDim.x / 32); ++w) {
+      err += sh[0][w];
+      err2 += sh[1][w];
+    }
+    double deno = err + 0.01 * err2;
+    if (deno <= 0.0) deno = 1.0;
+    out[0] = dt * err * sqrt(1.0 / (ntot * deno));
+    out[1] = rs->rho_mean;
+    out[2] = (rs->nonfinite || !isfinite(out[0])) ? 1.0 : 0.0;
+  }
+}
+
+static unsigned stream_grid(long long nvec) {
+  // a multiple of the 152 SMs, at most 8 CTAs per SM
+  long long b = (nvec + 255) / 256;
+  long long cap = 152LL * 8;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+static int lincomb(Ctx *c, const Vec &base, Vec &out, const LinArgs &args) {
+  const long long nf = c->g.Nf;
+  prof_begin(c, KK_LINCOMB);
+  if (c->mixed) {
+    k_lincomb<float><<<stream_grid(nf / 4), 256, 0, c->stream>>>(
+        (const float *)base.fl, base.sc, (float *)out.fl, out.sc, args, nf);
+  } else {
+    k_lincomb<double><<<stream_grid(nf / 2), 256, 0, c->stream>>>(
+        (const double *)base.fl, base.sc, (double *)out.fl, out.sc, args, nf);
+  }
+  prof_end(c, KK_LINCOMB, (double)(args.n + 2) * nf * c->tsize);
+  return check_launch(c, "k_lincomb");
+}
+
+static int alloc_vec(Ctx *c, Vec &v) {
+  if (v.fl) return IH_OK;
+  IH_CUDA(c, cudaMalloc(&v.fl, c->tsize * c->g.Nf));
+  IH_CUDA(c, cudaMemsetAsync(v.fl, 0, c->tsize * c->g.Nf, c->stream));
+  IH_CUDA(c, cudaMalloc((void **)&v.sc, sizeof(double) * kSc));
+  IH_CUDA(c, cudaMemsetAsync(v.sc, 0, sizeof(double) * kSc, c->stream));
+  c->dev_bytes += c->tsize * c->g.Nf + sizeof(double) * kSc;
+  return IH_OK;
+}
+
+int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0) {
+  tableau_init();
+  for (int j = 1; j <= 12; ++j) IH_TRY(alloc_vec(c, c->k[j]));
+  c->cfg = *cfg;
+  c->t = t0;
+  c->dt_next = dt0;
+  c->err_old = 1.0e-4;
+  c->reject = 0;
+  c->n_ok = c->n_bad = c->n_stp = c->n_tries = 0;
+  // prepare_and_save_timeslice: RHS with the filter on (toolbox.c:96-104)
+  IH_TRY(rhs(c, t0, c->y, c->k[1], 1, 0, nullptr));
+  c->dopri_ready = 1;
+  return IH_OK;
+}
+
+// try_step + error (dopri853.c:331-486); returns err via *err_out
+static int try_step(Ctx *c, double dt, double *err_out, double *rho_mean_out, int *nonfinite) {
+  const double t = c->t;
+  for (int s = 1; s < 12; ++s) {  // stage s+1 from stages 1..s
+    LinArgs a;
+    memset(&a, 0, sizeof a);
+    int n = 0;
+    for (int j = 0; j < s; ++j) {
+      if (DA[s][j] == 0.0) continue;
+      a.in[n] = c->k[j + 1].fl;
+      a.insc[n] = c->k[j + 1].sc;
+      a.coef[n] = DA[s][j];
+      ++n;
+    }
+    a.n = n;
+    a.scale = dt;
+    IH_TRY(lincomb(c, c->y, c->ytmp, a));
+    const double ts = (s == 11) ? t + dt : t + DC[s] * dt;
+    IH_TRY(rhs(c, ts, c->ytmp, c->k[s + 1], 0, 0, nullptr));
+  }
+  FinalArgs f;
+  memset(&f, 0, sizeof f);
+  const int st[8] = {1, 6, 7, 8, 9, 10, 11, 12};
+  for (int j = 0; j < 8; ++j) {
+    const int sidx = st[j] - 1;
+    f.k[j] = c->k[st[j]].fl;
+    f.ksc[j] = c->k[st[j]].sc;
+    f.b[j] = DB[sidx];
+    double bhh = (st[j] == 1) ? DBHH[0] : (st[j] == 9) ? DBHH[1] : (st[j] == 12) ? DBHH[2] : 0.0;
+    f.e5[j] = DB[sidx] - bhh;
+    f.e3[j] = DE3[sidx];
+  }
+  f.dt = dt;
+  f.rtol = c->cfg.rtol;
+  f.atol = c->cfg.atol;
+  f.noise = c->mixed ? c->noise_eta * 5.9604644775390625e-8 : 0.0;  // eta * 2^-24
+  const long long nf = c->g.Nf;
+  const int W = c->mixed ? 4 : 2;
+  const unsigned nb = stream_grid(nf / W);
+  prof_begin(c, KK_DOPRI_FINAL);
+  if (c->mixed)
+    k_dopri_final<float><<<nb, 256, 0, c->stream>>>((const float *)c->y.fl, c->y.sc,
+                                                    (float *)c->ynew.fl, c->ynew.sc, f, c->g.N,
+                                                    nf, c->partials);
+  else
+    k_dopri_final<double><<<nb, 256, 0, c->stream>>>((const double *)c->y.fl, c->y.sc,
+                                                     (double *)c->ynew.fl, c->ynew.sc, f,
+                                                     c->g.N, nf, c->partials);
+  prof_end(c, KK_DOPRI_FINAL, 10.0 * nf * c->tsize);
+  IH_TRY(check_launch(c, "k_dopri_final"));
+  k_dopri_err_finish<<<1, 256, 0, c->stream>>>(c->partials, (int)nb, dt, (double)c->g.Ntot, c->rs,
+                                               c->diag + 4 * c->g.bins + 48);
+  IH_TRY(check_launch(c, "k_dopri_err_finish"));
+  IH_CUDA(c, cudaMemcpyAsync(c->hpin, c->diag + 4 * c->g.bins + 48, sizeof(double) * 3,
+                             cudaMemcpyDeviceToHost, c->stream));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  *err_out = c->hpin[0];
+  *rho_mean_out = c->hpin[1];
+  *nonfinite = c->hpin[2] != 0.0;
+  return IH_OK;
+}
+
+// success() (dopri853.c:505-540)
+static int success(Ctx *c, double err, double rho_mean, double *dt) {
+  const ih_dopri_cfg &g = c->cfg;
+  const double alpha = 1.0 / 8.0 - g.beta * 0.2;
+  double scale;
+  if (err <= 1.0) {
+    if (err == 0.0) {
+      scale = g.maxscale;
+    } else {
+      scale = g.safe * pow(err, -alpha) * pow(c->err_old, g.beta);
+      if (scale < g.minscale) scale = g.minscale;
+      if (scale > g.maxscale) scale = g.maxscale;
+    }
+    c->dt_next = c->reject ? (*dt) * fmin(scale, 1.0) : (*dt) * scale;
+    if (g.max_dt_hubble_fraction > 0.0) {
+      const double minstep = g.max_dt_hubble_fraction * sqrt(3.0 / rho_mean);
+      if (c->dt_next > minstep) c->dt_next = minstep;
+    }
+    c->err_old = fmax(err, 1.0e-4);
+    c->reject = 0;
+    return 1;
+  }
+  scale = fmax(g.safe * pow(err, -alpha), g.minscale);
+  (*dt) *= scale;
+  c->reject = 1;
+  return 0;
+}
+
+int dopri_step(Ctx *c, double dt_try, int want_output, ih_step_info *info) {
+  if (!c->dopri_ready) {
+    c->err = "ih_dopri853_init has not been called";
+    return IH_ERR_STATE;
+  }
+  double dt = dt_try;
+  int tries = 0;
+  double err = 0.0;
+  for (;;) {
+    double rho_mean;
+    int nonfinite;
+    IH_TRY(try_step(c, dt, &err, &rho_mean, &nonfinite));
+    ++tries;
+    ++c->n_tries;
+    c->last_err = err;
+    if (nonfinite) {
+      c->err = "non-finite value in the RHS reductions or the error norm";
+      if (info) info->status = IH_ERR_NAN;
+      return IH_ERR_NAN;
+    }
+    if (success(c, err, rho_mean, &dt)) break;
+    if (fabs(dt) <= fabs(c->t) * DBL_EPSILON) {
+      c->err = "step size underflow";
+      if (info) {
+        info->status = IH_ERR_UNDERFLOW;
+        info->tries = tries;
+      }
+      return IH_ERR_UNDERFLOW;
+    }
+  }
+  // post-step RHS with the filter on (dopri853.c:285-293) into k[2], then swap
+  IH_TRY(rhs(c, c->t + dt, c->ynew, c->k[2], 1, want_output, &c->y));
+  Vec tmp = c->y;
+  c->y = c->ynew;
+  c->ynew = tmp;
+  tmp = c->k[1];
+  c->k[1] = c->k[2];
+  c->k[2] = tmp;
+  c->t += dt;
+  if (info) {
+    info->t = c->t;
+    info->dt_did = dt;
+    info->dt_next = c->dt_next;
+    info->err = err;
+    info->tries = tries;
+    info->status = IH_OK;
+  }
+  return IH_OK;
+}
+
+// rk4.c:108-161 (one step)
+int rk4_step(Ctx *c, double dt, int want_output) {
+  for (int j = 1; j <= 4; ++j) IH_TRY(alloc_vec(c, c->k[j]));
+  const double t = c->t;
+  IH_TRY(rhs(c, t, c->y, c->k[1], 1, want_output, nullptr));
+  LinArgs a;
+  memset(&a, 0, sizeof a);
+  a.n = 1;
+  a.coef[0] = 0.5;
+  a.in[0] = c->k[1].fl;
+  a.insc[0] = c->k[1].sc;
+  a.scale = dt;
+  IH_TRY(lincomb(c, c->y, c->ytmp, a));
+  IH_TRY(rhs(c, t + dt / 2.0, c->ytmp, c->k[2], 0, 0, nullptr));
+  a.in[0] = c->k[2].fl;
+  a.insc[0] = c->k[2].sc;
+  IH_TRY(lincomb(c, c->y, c->ytmp, a));
+  IH_TRY(rhs(c, t + dt / 2.0, c->ytmp, c->k[3], 0, 0, nullptr));
+  a.in[0] = c->k[3].fl;
+  a.insc[0] = c->k[3].sc;
+  a.coef[0] = 1.0;
+  IH_TRY(lincomb(c, c->y, c->ytmp, a));
+  IH_TRY(rhs(c, t + dt, c->ytmp, c->k[4], 0, 0, nullptr));
+  LinArgs f;
+  memset(&f, 0, sizeof f);
+  f.n = 4;
+  const double w[4] = {1.0 / 6.0, 2.0 / 6.0, 2.0 / 6.0, 1.0 / 6.0};
+  for (int j = 0; j < 4; ++j) {
+    f.in[j] = c->k[j + 1].fl;
+    f.insc[j] = c->k[j + 1].sc;
+    f.coef[j] = w[j];
+  }
+  f.scale = dt;
+  IH_TRY(lincomb(c, c->y, c->ynew, f));
+  Vec tmp = c->y;
+  c->y = c->ynew;
+  c->ynew = tmp;
+  c->t = t + dt;
+  return IH_OK;
+}
+
+}  // namespace ih

