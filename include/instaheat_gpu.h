@@ -133,6 +133,11 @@ int ih_get_field(ih_context *c, int which, double *out_host);
 int ih_get_output(ih_context *c, ih_output *out);
 unsigned long long ih_calls_rhs(const ih_context *c);
 
+/* mean (toolbox.c:726-734) of n doubles in device memory, FP64 two-stage
+ * reduction on the context stream (scratch: the context's partial-sum
+ * buffer).  *out_dev is device memory; the call returns once it is written. */
+int ih_mean_dev(ih_context *c, const double *f_dev, size_t n, double *out_dev);
+
 /* ---- transforms (fft / ifft, toolbox.c:806-827) on host buffers ----
  * r2c unnormalised exp(-i..) [x][y][z/2+1]; c2r unnormalised exp(+i..).
  * Computed in the context's precision. */

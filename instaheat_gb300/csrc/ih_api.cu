@@ -398,6 +398,15 @@ int ih_get_output(ih_context *h, ih_output *out) {
   return read_output(&h->c, out);
 }
 
+int ih_mean_dev(ih_context *h, const double *f_dev, size_t n, double *out_dev) {
+  CTX_CHECK(h);
+  if (!f_dev || !out_dev || n == 0) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  IH_TRY(reduce_mean_f64(c, f_dev, (long long)n, out_dev));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
 int ih_fft_host(ih_context *h, const double *in, double *out_c) {
   CTX_CHECK(h);
   if (!in || !out_c) return IH_ERR_ARG;

@@ -205,6 +205,7 @@ int fft_tables(Ctx *c);
 int rhs(Ctx *c, double t, Vec &y, Vec &k, int filter, int output,
         const Vec *smry_src);
 int reduce_mean(Ctx *c, const void *arr, long long n, double *dev_out);
+int reduce_mean_f64(Ctx *c, const double *arr, long long n, double *dev_out);
 int ic_fluctuations(Ctx *c, uint64_t seed, double phi0, double dphi0,
                     double a0, double amp, double kcut);
 int initial_psi(Ctx *c);

@@ -364,6 +364,10 @@ static int mean_into(Ctx *c, const T *a, long long n, double *dev_out) {
 
 __global__ void k_add_scalar(double *dst, const double *src) { *dst += *src; }
 
+int reduce_mean_f64(Ctx *c, const double *arr, long long n, double *dev_out) {
+  return mean_into<double>(c, arr, n, dev_out);
+}
+
 int reduce_mean(Ctx *c, const void *arr, long long n, double *dev_out) {
   if (c->mixed) return mean_into<float>(c, (const float *)arr, n, dev_out);
   return mean_into<double>(c, (const double *)arr, n, dev_out);

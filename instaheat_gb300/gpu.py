@@ -89,6 +89,7 @@ def load(build_if_missing: bool = True):
     L.ih_get_state.argtypes = [vp, _dp]
     L.ih_get_dstate.argtypes = [vp, _dp]
     L.ih_set_dstate.argtypes = [vp, _dp]
+    L.ih_mean_dev.argtypes = [vp, C.c_void_p, C.c_size_t, C.c_void_p]
     L.ih_time.restype = C.c_double
     L.ih_time.argtypes = [vp]
     L.ih_mk_rhs_host.argtypes = [vp, C.c_double, _dp, _dp, C.c_int, C.c_int]

@@ -204,3 +204,17 @@ def test_mixed_dopri_tracks_f64(gpu_mod, oracle_mod):
         scale = max(np.abs(ref - ref.mean()).max(), 1e-30)
         assert np.abs(got - ref).max() <= 1e-4 * scale + 1e-9 * abs(ref.mean()), s
     assert abs(fg[-1] / fo[-1] - 1) < 1e-9
+
+
+def test_mean_dev_matches_numpy(gpu_mod):
+    """ih_mean_dev (toolbox.c:726-734 on device memory)."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    ctx = gpu_mod.Context(n=(16, 16, 16))
+    x = torch.randn(1_000_003, dtype=torch.float64, device="cuda") + 0.25
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    st = ctx.L_.ih_mean_dev(ctx.h, C.c_void_p(x.data_ptr()), x.numel(), C.c_void_p(out.data_ptr()))
+    assert st == 0
+    ref = x.double().cpu().numpy().mean()
+    assert abs(out.item() - ref) <= 1e-13 * abs(ref)
