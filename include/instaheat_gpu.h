@@ -138,6 +138,7 @@ unsigned long long ih_calls_rhs(const ih_context *c);
  * buffer).  *out_dev is device memory; the call returns once it is written. */
 int ih_mean_dev(ih_context *c, const double *f_dev, size_t n, double *out_dev);
 
+
 /* ---- transforms (fft / ifft, toolbox.c:806-827) on host buffers ----
  * r2c unnormalised exp(-i..) [x][y][z/2+1]; c2r unnormalised exp(+i..).
  * Computed in the context's precision. */
@@ -186,10 +187,16 @@ int ih_rk4_step(ih_context *c, double dt, int want_output);
 /* Mixed form only: before an element of the two embedded error vectors enters
  * the FP64 error norm, its FP32 rounding floor eta * 2^-24 * sum_j |c_j k_j|
  * is subtracted from its magnitude (soft threshold), so that FP32 round-off
- * in the stage vectors does not drive the step size down.  Default eta = 32
+ * in the stage vectors does not drive the step size down.  Default eta = 256
  * in the mixed form; the plain FP64 form ignores it.  No reference
  * counterpart (the reference is FP64 only). */
 int ih_dopri853_set_noise_floor(ih_context *c, double eta);
+/* Diagnostic: with diag on, every try also sums the squared scaled error
+ * components per state segment; ih_dopri853_error_breakdown returns the last
+ * try's sums [phi, dphi, psi, dpsi, h1+h2, dh1+dh2] x (5th-order, 3rd-order)
+ * (the scale factor's share is the remainder of the total). */
+int ih_dopri853_diag_enable(ih_context *c, int on);
+int ih_dopri853_error_breakdown(ih_context *c, double *out12);
 
 /* ---- timing and instrumentation ---- */
 /* Synchronise the context's stream. */

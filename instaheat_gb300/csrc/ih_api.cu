@@ -639,6 +639,23 @@ int ih_host_free(void *p) {
   return IH_OK;
 }
 
+int ih_dopri853_diag_enable(ih_context *h, int on) {
+  CTX_CHECK(h);
+  h->c.err_diag = on ? 1 : 0;
+  return IH_OK;
+}
+
+int ih_dopri853_error_breakdown(ih_context *h, double *out12) {
+  CTX_CHECK(h);
+  if (!out12) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  if (!c->err_diag) return IH_ERR_STATE;
+  IH_CUDA(c, cudaMemcpyAsync(out12, c->diag + 4 * c->g.bins + 72, sizeof(double) * 12,
+                             cudaMemcpyDeviceToHost, c->stream));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
 int ih_dopri853_set_noise_floor(ih_context *h, double eta) {
   CTX_CHECK(h);
   if (!(eta >= 0.0)) return IH_ERR_ARG;

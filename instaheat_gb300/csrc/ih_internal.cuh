@@ -31,7 +31,7 @@ constexpr int kSc = 8;          // doubles of FP64 scalars per vector
 constexpr int kMaxPartials = 4096;
 // Mixed form: each FP32 error-vector element is soft-thresholded by
 // eta * eps32 * sum_j |c_j k_j| before it enters the FP64 error norm.
-constexpr double kDefaultNoiseEta = 32.0;
+constexpr double kDefaultNoiseEta = 256.0;
 
 template <typename T> struct Cplx;
 template <> struct Cplx<float> { using type = float2; };
@@ -134,6 +134,7 @@ struct Ctx {
   Timer timers[KK_COUNT];
   cudaEvent_t tev[2] = {nullptr, nullptr};  // ih_timer_start/stop
   double noise_eta = 0.0;       // FP32 rounding floor factor of the error norm
+  int err_diag = 0;             // per-segment error-norm breakdown on/off
 
   // last output flag results available
   int have_output = 0;

@@ -208,6 +208,8 @@ struct FinalArgs {
   double b[8], e5[8], e3[8];  // e5 = b - bhh on stages 1, 9, 12
   double dt, rtol, atol;
   double noise;               // eta * eps32 (mixed form), 0 for FP64
+  long long next;             // Next (tensor segment length)
+  double *diag;               // per-segment sums [phi, dphi, psi, dpsi, h, dh] x (e5, e3), or null
 };
 
 template <typename T>
@@ -242,6 +244,8 @@ __global__ void k_dopri_final(const T *__restrict__ y, const double *ysc, T *__r
   }
   const T dtT = (T)a.dt;
   double err = 0.0, err2 = 0.0;
+  double dacc[12];  // per-segment error sums (diagnostic mode only)
+  for (int i = 0; i < 12; ++i) dacc[i] = 0.0;
   for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
        v += (long long)gridDim.x * blockDim.x) {
     T ab[W], a5[W], a3[W], t5[W], t3[W], x[W];
@@ -287,7 +291,13 @@ __global__ void k_dopri_final(const T *__restrict__ y, const double *ysc, T *__r
       }
       err2 += (double)acc5;
       err += (double)acc3;
+      if (a.diag) {
+        const int cls = seg < 4 ? seg : (i0 < 4 * N + 2 * a.next ? 4 : 5);
+        dacc[2 * cls] += (double)acc5;
+        dacc[2 * cls + 1] += (double)acc3;
+      }
     } else {
+      double v5 = 0.0, v3 = 0.0;
 #pragma unroll
       for (int w = 0; w < W; ++w) {
         double yf = (double)yv[w], ynf = (double)yn[w], q5 = (double)a5[w], q3 = (double)a3[w];
@@ -299,10 +309,21 @@ __global__ void k_dopri_final(const T *__restrict__ y, const double *ysc, T *__r
         }
         const double sk = a.atol + a.rtol * fmax(fabs(yf), fabs(ynf));
         const double r5 = q5 / sk, r3 = q3 / sk;
-        err2 += r5 * r5;
-        err += r3 * r3;
+        v5 += r5 * r5;
+        v3 += r3 * r3;
+      }
+      err2 += v5;
+      err += v3;
+      if (a.diag) {
+        const int cls = seg < 4 ? seg : (i0 < 4 * N + 2 * a.next ? 4 : 5);
+        dacc[2 * cls] += v5;
+        dacc[2 * cls + 1] += v3;
       }
     }
+  }
+  if (a.diag) {
+    for (int i = 0; i < 12; ++i)
+      if (dacc[i] != 0.0) atomicAdd(&a.diag[i], dacc[i]);
   }
   // scale factor a (the last state component)
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -454,6 +475,12 @@ static int try_step(Ctx *c, double dt, double *err_out, double *rho_mean_out, in
   f.rtol = c->cfg.rtol;
   f.atol = c->cfg.atol;
   f.noise = c->mixed ? c->noise_eta * 5.9604644775390625e-8 : 0.0;  // eta * 2^-24
+  f.next = c->g.Next;
+  f.diag = nullptr;
+  if (c->err_diag) {
+    f.diag = c->diag + 4 * c->g.bins + 64 + 8;  // 12 doubles
+    IH_CUDA(c, cudaMemsetAsync(f.diag, 0, sizeof(double) * 12, c->stream));
+  }
   const long long nf = c->g.Nf;
   const int W = c->mixed ? 4 : 2;
   const unsigned nb = stream_grid(nf / W);

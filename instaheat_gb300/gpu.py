@@ -125,6 +125,8 @@ def load(build_if_missing: bool = True):
     L.ih_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     L.ih_host_free.argtypes = [C.c_void_p]
     L.ih_dopri853_set_noise_floor.argtypes = [vp, C.c_double]
+    L.ih_dopri853_diag_enable.argtypes = [vp, C.c_int]
+    L.ih_dopri853_error_breakdown.argtypes = [vp, _dp]
     _lib = L
     return L
 
@@ -348,6 +350,16 @@ class Context:
 
     def profile(self, on=True):
         self._ck(self.L_.ih_profile_enable(self.h, int(on)), "ih_profile_enable")
+
+    def error_breakdown(self, enable=None):
+        """Per-segment error sums of the last try (enable=True/False toggles)."""
+        if enable is not None:
+            self._ck(self.L_.ih_dopri853_diag_enable(self.h, int(enable)), "ih_dopri853_diag_enable")
+            return None
+        out = np.zeros(12)
+        self._ck(self.L_.ih_dopri853_error_breakdown(self.h, _ptr(out)), "ih_dopri853_error_breakdown")
+        names = ["phi", "dphi", "psi", "dpsi", "h", "dh"]
+        return {n: (out[2 * i], out[2 * i + 1]) for i, n in enumerate(names)}
 
     def set_noise_floor(self, eta):
         self._ck(self.L_.ih_dopri853_set_noise_floor(self.h, eta), "ih_dopri853_set_noise_floor")
