@@ -41,7 +41,8 @@ enum {
     IH_ERR_ALLOC = 3,      /* device or host allocation failed */
     IH_ERR_STATE = 4,      /* call out of order (e.g. step before init) */
     IH_ERR_UNDERFLOW = 5,  /* DOPRI853 step-size underflow (dopri853.c:280-283) */
-    IH_ERR_NAN = 6         /* non-finite value in a reduction (NaN/Inf flag) */
+    IH_ERR_NAN = 6,        /* non-finite value in a reduction (NaN/Inf flag) */
+    IH_ERR_TOO_LARGE = 7   /* input larger than a fixed-size entry point accepts */
 };
 
 enum { IH_PREC_F64 = 0, IH_PREC_MIXED = 1 };
@@ -138,6 +139,21 @@ unsigned long long ih_calls_rhs(const ih_context *c);
  * buffer).  *out_dev is device memory; the call returns once it is written. */
 int ih_mean_dev(ih_context *c, const double *f_dev, size_t n, double *out_dev);
 
+/* The same mean without allocating anything, for callers that cannot call
+ * cudaMalloc where they need it (a host program that gives all device memory
+ * to its own arena up front, a loop that must not pay or risk an allocation,
+ * code without an ih_context).  No counterpart in the reference.
+ * Scratch is a fixed 32 KiB array inside the library (held on every GPU that
+ * loads it until the process exits); it is shared by all calls, so calls that
+ * overlap on the GPU race and must be serialised by the caller.  The device
+ * address of that array is looked up once per device by the first call made
+ * on it, so make that first call before any stream capture.  n is limited to
+ * ih_mean_dev_noalloc_max_n() = 2^28 doubles; larger n returns
+ * IH_ERR_TOO_LARGE without launching anything.  Runs on `stream` (a
+ * cudaStream_t; NULL = the legacy default stream) and returns without
+ * waiting; *out_dev is device memory. */
+int ih_mean_dev_noalloc(const double *f_dev, size_t n, double *out_dev, void *stream);
+size_t ih_mean_dev_noalloc_max_n(void);
 
 /* ---- transforms (fft / ifft, toolbox.c:806-827) on host buffers ----
  * r2c unnormalised exp(-i..) [x][y][z/2+1]; c2r unnormalised exp(+i..).

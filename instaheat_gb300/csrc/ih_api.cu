@@ -242,6 +242,7 @@ const char *ih_status_string(int s) {
     case IH_ERR_STATE: return "call out of order";
     case IH_ERR_UNDERFLOW: return "step size underflow";
     case IH_ERR_NAN: return "non-finite value";
+    case IH_ERR_TOO_LARGE: return "input larger than the fixed scratch of this entry point allows";
     default: return "unknown status";
   }
 }
