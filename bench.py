@@ -215,6 +215,36 @@ def bench_e2e(gpu, ctx, steps):
             "d2h_bytes_per_step": 16 * Ntot, "ms_per_step": 1e3 * wall / steps}
 
 
+def accuracy_check(gpu, device, seed, t_end):
+    """Both forms from the same initial data to t_end (the last step lands on
+    t_end): GW spectrum and constraint residuals of the final states, and the
+    wall time of each run (an equal-span speed ratio)."""
+    runs = {}
+    for name, prec in (("mixed", gpu.PREC_MIXED), ("f64", gpu.PREC_F64)):
+        ctx = make_context(gpu, prec, device)
+        init_workload(ctx, gpu, seed)
+        ctx.sync()
+        t0 = time.perf_counter()
+        n, _ = ctx.dopri_run(t_end)
+        ctx.sync()
+        wall = time.perf_counter() - t0
+        d = ctx.prepare_output()
+        runs[name] = dict(gw=d["gw"], cstr=d["cstr"], steps=n, wall=wall,
+                          tries=ctx.dopri_counters()["tries"], t=ctx.t)
+        ctx.close()
+    gm, gf = runs["mixed"]["gw"], runs["f64"]["gw"]
+    sig = gf > 1e-3 * gf.max()
+    rel = np.abs(gm - gf)[sig] / gf[sig]
+    return {"t_end": t_end,
+            "gw_max_rel_diff": float(rel.max()), "gw_bins_compared": int(sig.sum()),
+            "cstr_mixed": [float(x) for x in runs["mixed"]["cstr"]],
+            "cstr_f64": [float(x) for x in runs["f64"]["cstr"]],
+            "steps": {k: runs[k]["steps"] for k in runs}, "tries": {k: runs[k]["tries"] for k in runs},
+            "wall_s": {k: runs[k]["wall"] for k in runs},
+            "speedup_equal_span": runs["f64"]["wall"] / runs["mixed"]["wall"],
+            "within_1pct": bool(rel.max() < 0.01)}
+
+
 def cpu_baseline_sample(threads=None):
     """One DOPRI853 step of the 256^3 workload with the CPU oracle."""
     from oracle import oracle as orc
@@ -244,6 +274,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
+    ap.add_argument("--accuracy-t", type=float, default=0.5,
+                    help="span of the mixed-vs-FP64 accuracy check (0 disables)")
     args = ap.parse_args()
     steps, warmup = args.steps, max(args.warmup, 3) if args.impl == "ours" else args.warmup
     dist = Dist()
@@ -291,6 +323,9 @@ def main():
     tfile = ROOT / "profiles" / "traffic_256.json"
     if tfile.exists():
         traffic = json.loads(tfile.read_text()).get(dname)
+    acc = None
+    if args.accuracy_t > 0 and not args.no_f64:
+        acc = accuracy_check(gpu, device, seed, args.accuracy_t)
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample()
@@ -325,6 +360,8 @@ def main():
             line["f64"] = {"value": f64v, "unit": UNIT, "ms_per_step": f64["ms"] / max(1, min(steps, 3)),
                            "dt_next": f64["dt_next"]}
             line["speedup_vs_f64"] = value / f64v
+        if acc:
+            line["accuracy_vs_f64"] = acc
         print(json.dumps(line), flush=True)
     dist.close()
 

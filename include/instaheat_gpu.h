@@ -132,6 +132,10 @@ int ih_get_means(const ih_context *c, double *rho_mean, double *pressure_mean);
  * which = 0 rho, 1 pressure, 2 laplacian of phi, 3 squared gradient. */
 int ih_get_field(ih_context *c, int which, double *out_host);
 int ih_get_output(ih_context *c, ih_output *out);
+/* prepare_and_save_timeslice without save() (toolbox.c:96-104): the RHS of
+ * the device state with filter = output = 1; dfield is updated, the state is
+ * filtered in place, the diagnostics are kept for ih_get_output. */
+int ih_prepare_output(ih_context *c);
 unsigned long long ih_calls_rhs(const ih_context *c);
 
 /* mean (toolbox.c:726-734) of n doubles in device memory, FP64 two-stage

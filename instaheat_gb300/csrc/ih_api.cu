@@ -116,6 +116,13 @@ static void make_geom(const ih_params *p, Geom *g) {
   g->kzmax = (p->nz / 2) * g->kzu;
   g->mass = p->mass;
   g->bins = p->bins;
+  int l = 0;
+  while ((1 << l) < g->mz) ++l;
+  g->mz_shift = l;
+  g->mz_magic = (unsigned)((((unsigned long long)1 << 32) * (((unsigned long long)1 << l) - g->mz)) /
+                               g->mz + 1);
+  g->logny = 0;
+  while ((1 << g->logny) < g->ny) ++g->logny;
 }
 
 static int dmalloc(Ctx *c, void **p, size_t bytes) {
@@ -637,6 +644,18 @@ int ih_host_alloc(size_t bytes, void **out) {
 
 int ih_host_free(void *p) {
   if (p && cudaFreeHost(p) != cudaSuccess) return IH_ERR_CUDA;
+  return IH_OK;
+}
+
+int ih_prepare_output(ih_context *h) {
+  CTX_CHECK(h);
+  Ctx *c = &h->c;
+  if (!c->have_state) {
+    c->err = "no state";
+    return IH_ERR_STATE;
+  }
+  IH_TRY(rhs(c, c->t, c->y, c->k[1], 1, 1, nullptr));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
   return IH_OK;
 }
 

@@ -49,6 +49,10 @@ struct Geom {
   double kxmax, kymax, kzmax;   // filter denominators, setup.c:712-714
   double mass;
   int bins;
+  // id / mz for 32-bit ids as (umulhi(id, mz_magic) + id) >> mz_shift
+  // (division by an invariant integer, Granlund-Montgomery); ny = 1 << logny
+  unsigned mz_magic;
+  int mz_shift, logny;
 };
 
 // RHS scalars produced on the device by the reduction-finish kernel.

@@ -224,7 +224,7 @@ __global__ void k_update_phi_psi(const T *__restrict__ y, const double *ysc,
                                  T *__restrict__ out, const RhsScalars *rs,
                                  long long N, double mass) {
   const double a2d = rs->a2, Hd = rs->H, pmd = rs->p_mean;
-  const T a2 = (T)a2d, H = (T)Hd, h3 = (T)(3.0 * Hd), pm = (T)pmd;
+  const T inv_a2 = (T)(1.0 / a2d), H = (T)Hd, h3 = (T)(3.0 * Hd), pm = (T)pmd;
   const T m2 = (T)(mass * mass);
   T phib = 0, pib = 0, psib = 0, dpsib = 0;
   if (MIXED) {
@@ -240,12 +240,12 @@ __global__ void k_update_phi_psi(const T *__restrict__ y, const double *ysc,
     out[i] = dph;
     out[2 * N + i] = dps;
     if (!MIXED) {
-      out[N + i] = ((T)1.0 + (T)4.0 * ps) * l / a2 - (h3 - (T)4.0 * dps) * dph -
+      out[N + i] = ((T)1.0 + (T)4.0 * ps) * l * inv_a2 - (h3 - (T)4.0 * dps) * dph -
                    ((T)1.0 + (T)2.0 * ps) * (m2 * ph);
       out[3 * N + i] = (T)0.5 * pp + (ps - (T)0.5) * pm - (T)4.0 * H * dps;
     } else {
       T psf = psib + ps, dpsf = dpsib + dps;
-      out[N + i] = ((T)1.0 + (T)4.0 * psf) * l / a2 + (T)4.0 * dps * pib -
+      out[N + i] = ((T)1.0 + (T)4.0 * psf) * l * inv_a2 + (T)4.0 * dps * pib -
                    (h3 - (T)4.0 * dpsf) * dph - (T)2.0 * ps * m2 * phib -
                    ((T)1.0 + (T)2.0 * psf) * m2 * ph;
       out[3 * N + i] = (T)0.5 * pp + ps * pm - (T)4.0 * H * dps;
@@ -260,12 +260,22 @@ __global__ void k_update_h(const C2<T> *__restrict__ s, const T *__restrict__ y,
                            T *__restrict__ out, const RhsScalars *rs, Geom g) {
   const long long M = g.M, N = g.N, Next = g.Next;
   const long long Nh1 = 4 * N, Nh2 = Nh1 + Next, Ndh1 = Nh2 + Next, Ndh2 = Ndh1 + Next;
-  const T a2 = (T)rs->a2, h3 = (T)(3.0 * rs->H), pm2 = (T)(2.0 * rs->p_mean);
+  const T inv_a2 = (T)(1.0 / rs->a2), two_inv_a2 = (T)(2.0 / rs->a2);
+  const T h3 = (T)(3.0 * rs->H), pm2 = (T)(2.0 * rs->p_mean);
   const C2<T> *s0 = s, *s1 = s + M, *s2 = s + 2 * M, *s3 = s + 3 * M;
   const C2<T> *s4 = s + 5 * M, *s5 = s + 6 * M;
+  const unsigned mz_magic = g.mz_magic;
+  const int mz_shift = g.mz_shift, logny = g.logny;
   for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < M;
        id += (long long)gridDim.x * blockDim.x) {
-    Mode m = mode_of(id, g);
+    // mode (i, j, k) of the half spectrum: one division by mz via a
+    // multiply-high (32-bit ids: M < 2^31)
+    const unsigned uid = (unsigned)id;
+    const unsigned r = (__umulhi(uid, mz_magic) + uid) >> mz_shift;
+    Mode m;
+    m.k = (int)(uid - r * (unsigned)g.mz);
+    m.j = (int)(r & (unsigned)(g.ny - 1));
+    m.i = (int)(r >> logny);
     C2<T> n0 = mk2c<T>(0, 0), n1 = mk2c<T>(0, 0);
     T ksq;
     if (id != 0) {
@@ -285,7 +295,8 @@ __global__ void k_update_h(const C2<T> *__restrict__ s, const T *__restrict__ y,
         ksq += (float)g.kx2 * (float)ia * (float)ia;
         ksq += (float)g.ky2 * (float)ja * (float)ja;
       }
-      const T fx = kx / ksq, fy = ky / ksq, fz = kz / ksq;
+      const T inv_ksq = (T)1.0 / ksq;
+      const T fx = kx * inv_ksq, fy = ky * inv_ksq, fz = kz * inv_ksq;
       C2<T> v0 = s0[id], v1 = s1[id], v2 = s2[id], v3 = s3[id], v4 = s4[id], v5 = s5[id];
 #define CL(c, a, b) mk2c<T>(a.x c b.x, a.y c b.y)
 #define SC(f, a) mk2c<T>((f) * a.x, (f) * a.y)
@@ -293,12 +304,14 @@ __global__ void k_update_h(const C2<T> *__restrict__ s, const T *__restrict__ y,
                     SC((T)2.0, CL(+, CL(+, SC(kx * fy, v1), SC(kx * fz, v2)), SC(ky * fz, v4))));
       C2<T> t2 = CL(+, CL(+, v0, v3), v5);
       C2<T> S1 = CL(+, t1, t2), S2 = CL(-, t1, t2);
-      if (fabs((double)kz) > DBL_EPSILON) {
+      // |kz| > DBL_EPSILON and |ky| > DBL_EPSILON of toolbox.c:377, 382: the
+      // grid components are either exactly 0 or at least 2 pi / L
+      if (m.k != 0) {
         C2<T> k1 = CL(+, CL(+, SC(kx, v0), SC(ky, v1)), SC(kz, v2));
         C2<T> k2 = CL(+, CL(+, SC(kx, v1), SC(ky, v3)), SC(kz, v4));
         n0 = CL(+, CL(-, v0, SC((T)2.0 * fx, k1)), SC((T)0.5, CL(+, SC(fx * kx, S1), S2)));
         n1 = CL(+, CL(-, CL(-, v1, SC(fx, k2)), SC(fy, k1)), SC((T)0.5 * fx * ky, S1));
-      } else if (fabs((double)ky) > DBL_EPSILON) {
+      } else if (m.j != 0) {
         C2<T> k1 = CL(+, CL(+, SC(kx, v0), SC(ky, v1)), SC(kz, v2));
         C2<T> k3 = CL(+, CL(+, SC(kx, v2), SC(ky, v4)), SC(kz, v5));
         n0 = CL(+, CL(-, v0, SC((T)2.0 * fx, k1)), SC((T)0.5, CL(+, SC(fx * kx, S1), S2)));
@@ -314,16 +327,19 @@ __global__ void k_update_h(const C2<T> *__restrict__ s, const T *__restrict__ y,
     } else {
       ksq = 0;
     }
-    const T tm = -(pm2 + ksq / a2);
-    const long long i1 = 2 * id, i2 = i1 + 1;
-    out[Nh1 + i1] = y[Ndh1 + i1];
-    out[Nh1 + i2] = y[Ndh1 + i2];
-    out[Nh2 + i1] = y[Ndh2 + i1];
-    out[Nh2 + i2] = y[Ndh2 + i2];
-    out[Ndh1 + i1] = tm * y[Nh1 + i1] - h3 * y[Ndh1 + i1] + (T)2.0 * n0.x / a2;
-    out[Ndh1 + i2] = tm * y[Nh1 + i2] - h3 * y[Ndh1 + i2] + (T)2.0 * n0.y / a2;
-    out[Ndh2 + i1] = tm * y[Nh2 + i1] - h3 * y[Ndh2 + i1] + (T)2.0 * n1.x / a2;
-    out[Ndh2 + i2] = tm * y[Nh2 + i2] - h3 * y[Ndh2 + i2] + (T)2.0 * n1.y / a2;
+    const T tm = -(pm2 + ksq * inv_a2);
+    const long long i1 = 2 * id;
+    typedef C2<T> V;
+    const V *yv = reinterpret_cast<const V *>(y);
+    V *ov = reinterpret_cast<V *>(out);
+    const V h1 = yv[(Nh1 + i1) / 2], h2 = yv[(Nh2 + i1) / 2];
+    const V d1 = yv[(Ndh1 + i1) / 2], d2 = yv[(Ndh2 + i1) / 2];
+    ov[(Nh1 + i1) / 2] = d1;
+    ov[(Nh2 + i1) / 2] = d2;
+    ov[(Ndh1 + i1) / 2] = mk2c<T>(tm * h1.x - h3 * d1.x + two_inv_a2 * n0.x,
+                                  tm * h1.y - h3 * d1.y + two_inv_a2 * n0.y);
+    ov[(Ndh2 + i1) / 2] = mk2c<T>(tm * h2.x - h3 * d2.x + two_inv_a2 * n1.x,
+                                  tm * h2.y - h3 * d2.y + two_inv_a2 * n1.y);
   }
 }
 

@@ -126,6 +126,7 @@ def load(build_if_missing: bool = True):
     L.ih_host_free.argtypes = [C.c_void_p]
     L.ih_dopri853_set_noise_floor.argtypes = [vp, C.c_double]
     L.ih_dopri853_diag_enable.argtypes = [vp, C.c_int]
+    L.ih_prepare_output.argtypes = [vp]
     L.ih_dopri853_error_breakdown.argtypes = [vp, _dp]
     _lib = L
     return L
@@ -277,6 +278,11 @@ class Context:
         out = np.zeros(self.N)
         self._ck(self.L_.ih_get_field(self.h, names[which], _ptr(out)), "ih_get_field")
         return out
+
+    def prepare_output(self):
+        """Diagnostics of the device state (prepare_and_save_timeslice)."""
+        self._ck(self.L_.ih_prepare_output(self.h), "ih_prepare_output")
+        return self.output()
 
     def output(self):
         b = self.bins
