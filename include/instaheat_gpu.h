@@ -199,6 +199,42 @@ int ih_dopri853_counters(const ih_context *c, double *dt_next, long *n_ok,
 int ih_dopri853_tableau(double *c, double *a, double *b, double *bhh,
                         double *er);
 
+/* ---- learned step-size proposer (no reference counterpart) ----
+ * A 12 -> 64 -> 64 -> 1 MLP (GELU), BF16 weights, FP32 accumulation, trained
+ * on the GPU by Adam.  Input features of accepted step n (ih_step_features):
+ * log dt_n..dt_{n-3}, log err_n..err_{n-3} (accepted tries), log a, H,
+ * log rms(delta phi), log rms(delta psi); output log dt_{n+1}.  With a
+ * proposer set, the step size after an accepted step is its proposal (clamped
+ * to [minscale, maxscale] x dt and to the Hubble cap); DOPRI853's error
+ * estimate still accepts or rejects every try, and a rejected proposal is
+ * reduced by the reference controller (dopri853.c:534-538). */
+#define IH_MLP_INPUTS 12
+#define IH_MLP_NPARAMS 5057
+typedef struct ih_mlp ih_mlp;
+int ih_mlp_create(int device, unsigned seed, ih_mlp **out);
+void ih_mlp_destroy(ih_mlp *m);
+const char *ih_mlp_last_error(const ih_mlp *m);
+/* FP32 master parameters: W1[12][64], b1[64], W2[64][64], b2[64], W3[64], b3 */
+int ih_mlp_set_params(ih_mlp *m, const float *params);
+int ih_mlp_get_params(ih_mlp *m, float *params);
+/* the BF16-rounded copy the forward and backward passes use */
+int ih_mlp_get_bf16_params(ih_mlp *m, float *params);
+/* x_norm = (x - in_mean) / in_std; log dt = out * out_std + out_mean */
+int ih_mlp_set_norm(ih_mlp *m, const float *in_mean, const float *in_std, float out_mean,
+                    float out_std);
+int ih_mlp_forward(ih_mlp *m, const float *x, int n, float *y);
+/* full-batch gradient of the mean squared error (normalised output units) */
+int ih_mlp_gradients(ih_mlp *m, const float *x, const float *y, int n, float *grad,
+                     float *loss);
+/* Adam (beta 0.9 / 0.999), `iters` minibatches of `batch` <= 128 rows drawn
+ * with a counter-based generator; loss_hist (iters floats) may be NULL */
+int ih_mlp_train(ih_mlp *m, const float *x, const float *y, int n, int iters, int batch,
+                 float lr, unsigned seed, float *loss_hist);
+/* the feature vector of the last accepted step (12 floats) */
+int ih_step_features(ih_context *c, float *out12);
+/* set (or with NULL clear) the proposer of a context */
+int ih_dopri853_set_proposer(ih_context *c, ih_mlp *m);
+
 /* ---- RK4 (rk4.c:27-132) ---- */
 /* One step of size dt from the context time; the stage-1 RHS runs with
  * filter=1 and, if want_output, output=1 (rk4.c:63-75). */

@@ -202,6 +202,7 @@ static void destroy(Ctx *c) {
   if (c->diag) cudaFree(c->diag);
   if (c->hpin) cudaFreeHost(c->hpin);
   if (c->stage_dev) cudaFree(c->stage_dev);
+  if (c->feat_dev) cudaFree(c->feat_dev);
   free_vec(c->y);
   free_vec(c->ynew);
   free_vec(c->ytmp);
@@ -644,6 +645,20 @@ int ih_host_alloc(size_t bytes, void **out) {
 
 int ih_host_free(void *p) {
   if (p && cudaFreeHost(p) != cudaSuccess) return IH_ERR_CUDA;
+  return IH_OK;
+}
+
+int ih_step_features(ih_context *h, float *out12) {
+  CTX_CHECK(h);
+  if (!out12) return IH_ERR_ARG;
+  return step_features(&h->c, out12);
+}
+
+int ih_dopri853_set_proposer(ih_context *h, ih_mlp *m) {
+  CTX_CHECK(h);
+  Ctx *c = &h->c;
+  if (m && !c->feat_dev) IH_TRY(dmalloc(c, (void **)&c->feat_dev, sizeof(float) * 16));
+  c->proposer = m;
   return IH_OK;
 }
 

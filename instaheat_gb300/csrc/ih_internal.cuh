@@ -139,6 +139,12 @@ struct Ctx {
   cudaEvent_t tev[2] = {nullptr, nullptr};  // ih_timer_start/stop
   double noise_eta = 0.0;       // FP32 rounding floor factor of the error norm
   int err_diag = 0;             // per-segment error-norm breakdown on/off
+  // accepted-step history (features of the learned proposer)
+  double hist_dt[4] = {0, 0, 0, 0}, hist_err[4] = {0, 0, 0, 0};
+  int hist_n = 0;
+  ih_mlp *proposer = nullptr;
+  float *feat_dev = nullptr;    // 16 floats: 12 features, output at [12]
+  double dt_next_pi = 0.0;      // the controller's own proposal of the last step
 
   // last output flag results available
   int have_output = 0;
@@ -223,6 +229,11 @@ int get_field(Ctx *c, int which, double *dev_out);
 int read_output(Ctx *c, ih_output *out);
 int mask_init(Ctx *c, void *mask);
 int convert_add(Ctx *c, const void *a, double add, long long n, double *out);
+
+// learned proposer (ih_mlp.cu, ih_stepper.cu)
+int mlp_forward_async(ih_mlp *m, const float *dx, int n, float *dy, cudaStream_t s);
+int step_features(Ctx *c, float *out12);
+int field_rms(Ctx *c, const void *arr, long long n, double *dev_out);
 
 // stepper (ih_stepper.cu)
 int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0);

@@ -380,6 +380,50 @@ static int mean_into(Ctx *c, const T *a, long long n, double *dev_out) {
 
 __global__ void k_add_scalar(double *dst, const double *src) { *dst += *src; }
 
+// sum and sum of squares per block -> rms about the mean (FP64)
+template <typename T>
+__global__ void k_partial_sum2(const T *a, long long n, double *partials) {
+  double s = 0.0, q = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double v = (double)a[i];
+    s += v;
+    q += v * v;
+  }
+  s = block_sum(s);
+  __syncthreads();
+  q = block_sum(q);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = s;
+    partials[2 * blockIdx.x + 1] = q;
+  }
+}
+__global__ void k_finish_rms(const double *partials, int nb, long long n, double *out) {
+  double s = 0.0, q = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    s += partials[2 * b];
+    q += partials[2 * b + 1];
+  }
+  s = block_sum(s);
+  __syncthreads();
+  q = block_sum(q);
+  if (threadIdx.x == 0) {
+    const double m = s / (double)n;
+    *out = sqrt(fmax(q / (double)n - m * m, 0.0));
+  }
+}
+
+int field_rms(Ctx *c, const void *arr, long long n, double *dev_out) {
+  const int nb = nblk_reduce(n);
+  if (c->mixed)
+    k_partial_sum2<float><<<nb, 256, 0, c->stream>>>((const float *)arr, n, c->partials);
+  else
+    k_partial_sum2<double><<<nb, 256, 0, c->stream>>>((const double *)arr, n, c->partials);
+  IH_TRY(check_launch(c, "k_partial_sum2"));
+  k_finish_rms<<<1, 256, 0, c->stream>>>(c->partials, nb, n, dev_out);
+  return check_launch(c, "k_finish_rms");
+}
+
 int reduce_mean_f64(Ctx *c, const double *arr, long long n, double *dev_out) {
   return mean_into<double>(c, arr, n, dev_out);
 }

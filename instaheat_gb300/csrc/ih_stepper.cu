@@ -424,6 +424,55 @@ static int alloc_vec(Ctx *c, Vec &v) {
   return IH_OK;
 }
 
+// Features of the last accepted step: log dt_n..dt_{n-3}, log err_n..err_{n-3},
+// log a, H, log rms(delta phi), log rms(delta psi).  Missing history entries
+// repeat the oldest available one.
+int step_features(Ctx *c, float *out) {
+  if (c->hist_n < 1) {
+    c->err = "no accepted step yet";
+    return IH_ERR_STATE;
+  }
+  double *d = c->diag + 4 * c->g.bins + 100;  // 2 doubles: rms phi, rms psi
+  IH_TRY(field_rms(c, c->y.fl, c->g.N, d));
+  IH_TRY(field_rms(c, (const char *)c->y.fl + 2 * c->g.N * c->tsize, c->g.N, d + 1));
+  IH_CUDA(c, cudaMemcpyAsync(c->hpin, d, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));
+  IH_CUDA(c, cudaMemcpyAsync(c->hpin + 2, c->y.sc + 4, sizeof(double), cudaMemcpyDeviceToHost,
+                             c->stream));
+  IH_CUDA(c, cudaMemcpyAsync(c->hpin + 3, (const char *)c->rs + offsetof(RhsScalars, H),
+                             sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  const int n = c->hist_n < 4 ? c->hist_n : 4;
+  for (int i = 0; i < 4; ++i) {
+    const int k = i < n ? i : n - 1;
+    out[i] = (float)log(c->hist_dt[k]);
+    out[4 + i] = (float)log(fmax(c->hist_err[k], 1e-10));
+  }
+  out[8] = (float)log(c->hpin[2]);
+  out[9] = (float)c->hpin[3];
+  out[10] = (float)log(fmax(c->hpin[0], 1e-300));
+  out[11] = (float)log(fmax(c->hpin[1], 1e-300));
+  return IH_OK;
+}
+
+// the learned proposal for the next step (after an accepted step)
+static int learned_dt(Ctx *c, double dt_did, double rho_mean, double *dt_out) {
+  float f[IH_MLP_INPUTS];
+  IH_TRY(step_features(c, f));
+  IH_CUDA(c, cudaMemcpyAsync(c->feat_dev, f, sizeof f, cudaMemcpyHostToDevice, c->stream));
+  IH_TRY(mlp_forward_async(c->proposer, c->feat_dev, 1, c->feat_dev + 12, c->stream));
+  float ylog = 0.f;
+  IH_CUDA(c, cudaMemcpyAsync(&ylog, c->feat_dev + 12, sizeof(float), cudaMemcpyDeviceToHost,
+                             c->stream));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  double dt = exp((double)ylog);
+  if (!(dt > 0.0) || !isfinite(dt)) dt = c->dt_next_pi;  // fall back to the controller
+  dt = fmin(fmax(dt, dt_did * c->cfg.minscale), dt_did * c->cfg.maxscale);
+  if (c->cfg.max_dt_hubble_fraction > 0.0)
+    dt = fmin(dt, c->cfg.max_dt_hubble_fraction * sqrt(3.0 / rho_mean));
+  *dt_out = dt;
+  return IH_OK;
+}
+
 int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0) {
   tableau_init();
   for (int j = 1; j <= 12; ++j) IH_TRY(alloc_vec(c, c->k[j]));
@@ -433,6 +482,7 @@ int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0) {
   c->err_old = 1.0e-4;
   c->reject = 0;
   c->n_ok = c->n_bad = c->n_stp = c->n_tries = 0;
+  c->hist_n = 0;
   // prepare_and_save_timeslice: RHS with the filter on (toolbox.c:96-104)
   IH_TRY(rhs(c, t0, c->y, c->k[1], 1, 0, nullptr));
   c->dopri_ready = 1;
@@ -542,9 +592,8 @@ int dopri_step(Ctx *c, double dt_try, int want_output, ih_step_info *info) {
   }
   double dt = dt_try;
   int tries = 0;
-  double err = 0.0;
+  double err = 0.0, rho_mean = 0.0;
   for (;;) {
-    double rho_mean;
     int nonfinite;
     IH_TRY(try_step(c, dt, &err, &rho_mean, &nonfinite));
     ++tries;
@@ -574,6 +623,16 @@ int dopri_step(Ctx *c, double dt_try, int want_output, ih_step_info *info) {
   c->k[1] = c->k[2];
   c->k[2] = tmp;
   c->t += dt;
+  // step history; with a proposer its proposal replaces the controller's
+  for (int i = 3; i > 0; --i) {
+    c->hist_dt[i] = c->hist_dt[i - 1];
+    c->hist_err[i] = c->hist_err[i - 1];
+  }
+  c->hist_dt[0] = dt;
+  c->hist_err[0] = err;
+  if (c->hist_n < 4) ++c->hist_n;
+  c->dt_next_pi = c->dt_next;
+  if (c->proposer) IH_TRY(learned_dt(c, dt, rho_mean, &c->dt_next));
   if (info) {
     info->t = c->t;
     info->dt_did = dt;

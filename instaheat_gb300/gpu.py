@@ -127,9 +127,109 @@ def load(build_if_missing: bool = True):
     L.ih_dopri853_set_noise_floor.argtypes = [vp, C.c_double]
     L.ih_dopri853_diag_enable.argtypes = [vp, C.c_int]
     L.ih_prepare_output.argtypes = [vp]
+    _fp = C.POINTER(C.c_float)
+    L.ih_mlp_create.argtypes = [C.c_int, C.c_uint, C.POINTER(vp)]
+    L.ih_mlp_destroy.argtypes = [vp]
+    L.ih_mlp_destroy.restype = None
+    L.ih_mlp_last_error.restype = C.c_char_p
+    L.ih_mlp_last_error.argtypes = [vp]
+    L.ih_mlp_set_params.argtypes = [vp, _fp]
+    L.ih_mlp_get_params.argtypes = [vp, _fp]
+    L.ih_mlp_get_bf16_params.argtypes = [vp, _fp]
+    L.ih_mlp_set_norm.argtypes = [vp, _fp, _fp, C.c_float, C.c_float]
+    L.ih_mlp_forward.argtypes = [vp, _fp, C.c_int, _fp]
+    L.ih_mlp_gradients.argtypes = [vp, _fp, _fp, C.c_int, _fp, _fp]
+    L.ih_mlp_train.argtypes = [vp, _fp, _fp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_uint, _fp]
+    L.ih_step_features.argtypes = [vp, _fp]
+    L.ih_dopri853_set_proposer.argtypes = [vp, vp]
     L.ih_dopri853_error_breakdown.argtypes = [vp, _dp]
     _lib = L
     return L
+
+
+MLP_INPUTS = 12
+MLP_NPARAMS = 5057
+
+
+def _fptr(a: np.ndarray):
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class MLP:
+    """The learned step-size proposer (ih_mlp): 12 -> 64 -> 64 -> 1, GELU,
+    BF16 weights with FP32 accumulation, trained on the GPU."""
+
+    def __init__(self, device=0, seed=0):
+        self.L_ = load()
+        h = C.c_void_p()
+        st = self.L_.ih_mlp_create(device, seed, C.byref(h))
+        if st:
+            raise IHError(st, "ih_mlp_create")
+        self.h = h
+        self.norm = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L_.ih_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, st, what):
+        if st:
+            raise IHError(st, f"{what}: {self.L_.ih_mlp_last_error(self.h).decode()}")
+
+    @property
+    def params(self):
+        p = np.zeros(MLP_NPARAMS, dtype=np.float32)
+        self._ck(self.L_.ih_mlp_get_params(self.h, _fptr(p)), "ih_mlp_get_params")
+        return p
+
+    @params.setter
+    def params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == MLP_NPARAMS
+        self._ck(self.L_.ih_mlp_set_params(self.h, _fptr(p)), "ih_mlp_set_params")
+
+    def bf16_params(self):
+        p = np.zeros(MLP_NPARAMS, dtype=np.float32)
+        self._ck(self.L_.ih_mlp_get_bf16_params(self.h, _fptr(p)), "ih_mlp_get_bf16_params")
+        return p
+
+    def set_norm(self, in_mean, in_std, out_mean, out_std):
+        m = np.ascontiguousarray(in_mean, dtype=np.float32)
+        s = np.ascontiguousarray(in_std, dtype=np.float32)
+        self._ck(self.L_.ih_mlp_set_norm(self.h, _fptr(m), _fptr(s), float(out_mean), float(out_std)),
+                 "ih_mlp_set_norm")
+        self.norm = (m.copy(), s.copy(), float(out_mean), float(out_std))
+
+    def forward(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, MLP_INPUTS)
+        y = np.zeros(len(X), dtype=np.float32)
+        self._ck(self.L_.ih_mlp_forward(self.h, _fptr(X), len(X), _fptr(y)), "ih_mlp_forward")
+        return y
+
+    def gradients(self, X, Y):
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, MLP_INPUTS)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        g = np.zeros(MLP_NPARAMS, dtype=np.float32)
+        loss = C.c_float()
+        self._ck(self.L_.ih_mlp_gradients(self.h, _fptr(X), _fptr(Y), len(X), _fptr(g), C.byref(loss)),
+                 "ih_mlp_gradients")
+        return g, loss.value
+
+    def train(self, X, Y, iters=2000, batch=128, lr=3e-3, seed=1):
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, MLP_INPUTS)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        hist = np.zeros(iters, dtype=np.float32)
+        self._ck(self.L_.ih_mlp_train(self.h, _fptr(X), _fptr(Y), len(X), iters, batch, lr, seed,
+                                      _fptr(hist)), "ih_mlp_train")
+        return hist
 
 
 class PinnedArray:
@@ -366,6 +466,16 @@ class Context:
         self._ck(self.L_.ih_dopri853_error_breakdown(self.h, _ptr(out)), "ih_dopri853_error_breakdown")
         names = ["phi", "dphi", "psi", "dpsi", "h", "dh"]
         return {n: (out[2 * i], out[2 * i + 1]) for i, n in enumerate(names)}
+
+    def step_features(self):
+        f = np.zeros(MLP_INPUTS, dtype=np.float32)
+        self._ck(self.L_.ih_step_features(self.h, _fptr(f)), "ih_step_features")
+        return f
+
+    def set_proposer(self, mlp):
+        self._proposer = mlp  # keep it alive while the context uses it
+        self._ck(self.L_.ih_dopri853_set_proposer(self.h, mlp.h if mlp is not None else None),
+                 "ih_dopri853_set_proposer")
 
     def set_noise_floor(self, eta):
         self._ck(self.L_.ih_dopri853_set_noise_floor(self.h, eta), "ih_dopri853_set_noise_floor")

@@ -1,0 +1,158 @@
+"""The learned step-size proposer: step logs, GPU training, model files.
+
+Why it exists: the mixed-precision form's DOPRI853 error estimate carries FP32
+round-off, so its controller alone does not reproduce the FP64 form's step
+sequence, and the reference's per-step spectral filter makes the GW spectrum
+depend on that sequence.  The proposer is trained to propose the FP64 form's
+next step size from what the mixed form itself observes; DOPRI853 still
+accepts or rejects every try and the reference controller handles rejections.
+
+Step logs: for each seed, the FP64 form runs with its own controller and logs
+its accepted step sizes; the mixed form then replays exactly those steps and
+records, after every step, its feature vector (ih_step_features: last four
+log dt, last four log error norms, log a, H, log rms delta phi, log rms
+delta psi).  Training pairs: features after step n -> log dt_{n+1} of FP64.
+
+    python -m instaheat_gb300.learned_dt --n 128,256 --seeds 1,2,3 --t-end 1.0 \\
+        --out instaheat_gb300/data/dt_mlp.json
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+from pathlib import Path
+
+import numpy as np
+
+from . import gpu
+
+DEFAULT_MODEL = Path(__file__).resolve().parent / "data" / "dt_mlp.json"
+
+
+def step_log(n, seed, t_end, rtol=1e-8, device=0, amp=1e-3):
+    """(X, Y, info) for one realization: mixed-form features replaying FP64."""
+    c64 = gpu.Context(n=(n,) * 3, precision=gpu.PREC_F64, device=device)
+    c64.ic(seed=seed, amp=amp)
+    c64.dopri_init(gpu.dopri_cfg(rtol, rtol), 0.0, 1e-3)
+    t0 = time.perf_counter()
+    steps, log = c64.dopri_run(t_end, log_cap=1_000_000)
+    w64 = time.perf_counter() - t0
+    c64.close()
+    dts = log[:, 1]
+    cm = gpu.Context(n=(n,) * 3, precision=gpu.PREC_MIXED, device=device)
+    cm.ic(seed=seed, amp=amp)
+    cm.dopri_init(gpu.dopri_cfg(rtol, rtol), 0.0, 1e-3)
+    X, Y = [], []
+    replayed = 0
+    for k in range(len(dts) - 1):
+        info = cm.dopri_step(dts[k])
+        if info.tries != 1 or info.dt_did != dts[k]:
+            break  # the mixed form rejected a FP64 step: the replay ends here
+        replayed += 1
+        if k + 1 < len(dts) - 1:  # the last FP64 step is truncated to land on t_end
+            X.append(cm.step_features())
+            Y.append(np.log(dts[k + 1]))
+    cm.close()
+    return (np.array(X, dtype=np.float32).reshape(-1, gpu.MLP_INPUTS), np.array(Y, dtype=np.float32),
+            {"n": n, "seed": seed, "steps_f64": int(steps), "replayed": replayed, "wall_f64_s": w64})
+
+
+def fit(X, Y, device=0, iters=3000, lr=3e-3, seed=1):
+    mean = X.mean(axis=0)
+    std = np.maximum(X.std(axis=0), 1e-3)
+    om, osd = float(Y.mean()), float(max(Y.std(), 1e-3))
+    mlp = gpu.MLP(device=device, seed=seed)
+    mlp.set_norm(mean, std, om, osd)
+    hist = mlp.train(X, Y, iters=iters, batch=128, lr=lr, seed=seed)
+    return mlp, hist
+
+
+def save(mlp, path, meta=None):
+    m, s, om, osd = mlp.norm
+    d = {"format": "instaheat_gb300 dt proposer v1", "params": [float(x) for x in mlp.params],
+         "in_mean": [float(x) for x in m], "in_std": [float(x) for x in s],
+         "out_mean": om, "out_std": osd, "meta": meta or {}}
+    Path(path).parent.mkdir(parents=True, exist_ok=True)
+    Path(path).write_text(json.dumps(d))
+
+
+def load(path=DEFAULT_MODEL, device=0):
+    d = json.loads(Path(path).read_text())
+    mlp = gpu.MLP(device=device)
+    mlp.params = np.array(d["params"], dtype=np.float32)
+    mlp.set_norm(np.array(d["in_mean"]), np.array(d["in_std"]), d["out_mean"], d["out_std"])
+    return mlp, d.get("meta", {})
+
+
+def evaluate(n, seed, t_end, model=DEFAULT_MODEL, rtol=1e-8, device=0, amp=1e-3):
+    """FP64 with its controller, mixed with the controller alone, and mixed
+    with the proposer, all to t_end from the same data: accepted steps, tries,
+    wall time, and the GW spectrum / constraints against the FP64 run."""
+    runs = {}
+    mlp, _ = load(model, device)
+    for name, prec, prop in (("f64", gpu.PREC_F64, None), ("mixed_pi", gpu.PREC_MIXED, None),
+                             ("mixed_learned", gpu.PREC_MIXED, mlp)):
+        ctx = gpu.Context(n=(n,) * 3, precision=prec, device=device)
+        ctx.ic(seed=seed, amp=amp)
+        ctx.dopri_init(gpu.dopri_cfg(rtol, rtol), 0.0, 1e-3)
+        if prop is not None:
+            ctx.set_proposer(prop)
+        ctx.sync()
+        t0 = time.perf_counter()
+        steps, _ = ctx.dopri_run(t_end)
+        ctx.sync()
+        wall = time.perf_counter() - t0
+        d = ctx.prepare_output()
+        runs[name] = {"steps": int(steps), "tries": int(ctx.dopri_counters()["tries"]), "wall_s": wall,
+                      "gw": d["gw"], "cstr": d["cstr"]}
+        ctx.close()
+    g64 = runs["f64"]["gw"]
+    sig = g64 > 1e-3 * g64.max()
+    out = {"n": n, "seed": seed, "t_end": t_end}
+    for k, r in runs.items():
+        rel = np.abs(r["gw"] - g64)[sig] / g64[sig]
+        out[k] = {"steps": r["steps"], "tries": r["tries"], "wall_s": r["wall_s"],
+                  "mt_per_s": t_end / r["wall_s"], "gw_max_rel_vs_f64": float(rel.max()),
+                  "cstr": [float(x) for x in r["cstr"]]}
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--evaluate", action="store_true", help="evaluate the saved model")
+    ap.add_argument("--eval-n", type=int, default=256)
+    ap.add_argument("--eval-seed", type=int, default=0)
+    ap.add_argument("--eval-t", type=float, default=0.5)
+    ap.add_argument("--n", default="128,256")
+    ap.add_argument("--seeds", default="1,2,3")
+    ap.add_argument("--t-end", type=float, default=1.0)
+    ap.add_argument("--iters", type=int, default=3000)
+    ap.add_argument("--lr", type=float, default=3e-3)
+    ap.add_argument("--out", default=str(DEFAULT_MODEL))
+    args = ap.parse_args(argv)
+    if args.evaluate:
+        print(json.dumps(evaluate(args.eval_n, args.eval_seed, args.eval_t, args.out)), flush=True)
+        return
+    Xs, Ys, infos = [], [], []
+    for n in [int(x) for x in args.n.split(",")]:
+        for s in [int(x) for x in args.seeds.split(",")]:
+            X, Y, info = step_log(n, s, args.t_end)
+            print(json.dumps(info), flush=True)
+            Xs.append(X)
+            Ys.append(Y)
+            infos.append(info)
+    X = np.concatenate(Xs)
+    Y = np.concatenate(Ys)
+    mlp, hist = fit(X, Y, iters=args.iters, lr=args.lr)
+    pred = mlp.forward(X)
+    rms = float(np.sqrt(np.mean((pred - Y) ** 2)))
+    meta = {"rows": int(len(X)), "runs": infos, "t_end": args.t_end, "iters": args.iters,
+            "lr": args.lr, "final_loss": float(hist[-50:].mean()), "rms_log_dt_error": rms}
+    save(mlp, args.out, meta)
+    print(json.dumps({"saved": args.out, "rows": len(X), "loss_first": float(hist[:50].mean()),
+                      "loss_last": float(hist[-50:].mean()), "rms_log_dt_error": rms}), flush=True)
+
+
+if __name__ == "__main__":
+    main()
