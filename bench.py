@@ -163,10 +163,17 @@ def run_steps(ctx, dt, k):
     return dt, mt
 
 
-def bench_form(gpu, precision, device, seed, steps, warmup, profile=False, clocks=None, dist=None):
+def bench_form(gpu, precision, device, seed, steps, warmup, profile=False, clocks=None, dist=None,
+               proposer=None, t_settle=0.1):
     ctx = make_context(gpu, precision, device)
     init_workload(ctx, gpu, seed)
-    dt, _ = run_steps(ctx, 1e-3, warmup)
+    if proposer is not None:
+        ctx.set_proposer(proposer)
+    # settle: advance past the step-size ramp from dt0 (untimed), then warm up
+    dt = 1e-3
+    while ctx.t < t_settle:
+        dt = ctx.dopri_step(dt).dt_next
+    dt, _ = run_steps(ctx, dt, warmup)
     ctx.sync()
     if dist:
         dist.barrier()
@@ -215,34 +222,18 @@ def bench_e2e(gpu, ctx, steps):
             "d2h_bytes_per_step": 16 * Ntot, "ms_per_step": 1e3 * wall / steps}
 
 
-def accuracy_check(gpu, device, seed, t_end):
-    """Both forms from the same initial data to t_end (the last step lands on
-    t_end): GW spectrum and constraint residuals of the final states, and the
-    wall time of each run (an equal-span speed ratio)."""
-    runs = {}
-    for name, prec in (("mixed", gpu.PREC_MIXED), ("f64", gpu.PREC_F64)):
-        ctx = make_context(gpu, prec, device)
-        init_workload(ctx, gpu, seed)
-        ctx.sync()
-        t0 = time.perf_counter()
-        n, _ = ctx.dopri_run(t_end)
-        ctx.sync()
-        wall = time.perf_counter() - t0
-        d = ctx.prepare_output()
-        runs[name] = dict(gw=d["gw"], cstr=d["cstr"], steps=n, wall=wall,
-                          tries=ctx.dopri_counters()["tries"], t=ctx.t)
-        ctx.close()
-    gm, gf = runs["mixed"]["gw"], runs["f64"]["gw"]
-    sig = gf > 1e-3 * gf.max()
-    rel = np.abs(gm - gf)[sig] / gf[sig]
-    return {"t_end": t_end,
-            "gw_max_rel_diff": float(rel.max()), "gw_bins_compared": int(sig.sum()),
-            "cstr_mixed": [float(x) for x in runs["mixed"]["cstr"]],
-            "cstr_f64": [float(x) for x in runs["f64"]["cstr"]],
-            "steps": {k: runs[k]["steps"] for k in runs}, "tries": {k: runs[k]["tries"] for k in runs},
-            "wall_s": {k: runs[k]["wall"] for k in runs},
-            "speedup_equal_span": runs["f64"]["wall"] / runs["mixed"]["wall"],
-            "within_1pct": bool(rel.max() < 0.01)}
+def accuracy_check(device, seed, t_end):
+    """FP64, mixed + controller alone, and mixed + learned proposer from the
+    same initial data to t_end (the last step lands on t_end): GW spectrum and
+    constraint residuals of the final states against the FP64 run, and each
+    run's wall time (an equal-span speed ratio)."""
+    from instaheat_gb300 import learned_dt
+    r = learned_dt.evaluate(N_GRID, seed, t_end, device=device)
+    ml = r["mixed_learned"]
+    return {"t_end": t_end, "runs": {k: r[k] for k in ("f64", "mixed_pi", "mixed_learned")},
+            "gw_max_rel_diff": ml["gw_max_rel_vs_f64"],
+            "speedup_equal_span": r["f64"]["wall_s"] / ml["wall_s"],
+            "within_1pct": bool(ml["gw_max_rel_vs_f64"] < 0.01)}
 
 
 def cpu_baseline_sample(threads=None):
@@ -300,8 +291,10 @@ def main():
     device = dist.local if dist.ws > 1 else 0
     seed = dist.rank
     clocks = Clocks(device)
+    from instaheat_gb300 import learned_dt
+    proposer, _ = learned_dt.load(device=device)  # the committed trained model
     ctx, mixed = bench_form(gpu, gpu.PREC_MIXED, device, seed, steps, warmup, profile=True,
-                            clocks=clocks, dist=dist)
+                            clocks=clocks, dist=dist, proposer=proposer)
     e2e = bench_e2e(gpu, ctx, max(2, min(steps, 5)))
     ctx.close()
     f64 = None
@@ -325,7 +318,7 @@ def main():
         traffic = json.loads(tfile.read_text()).get(dname)
     acc = None
     if args.accuracy_t > 0 and not args.no_f64:
-        acc = accuracy_check(gpu, device, seed, args.accuracy_t)
+        acc = accuracy_check(device, seed, args.accuracy_t)
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample()
@@ -338,8 +331,10 @@ def main():
             "data": "synthetic: seeded fluctuation initial data (amp 1e-3), psi from the constraints",
             "config": {"workload": "256^3 box L=20/m, V=m^2 phi^2/2, DOPRI853 rtol=atol=1e-8, GW on, "
                                    "filter on; mixed FP32 fields/FFTs + FP64 k=0 parts, a, H, "
-                                   "reductions and error norm; PI controller",
-                       "grid": N_GRID, "rtol": RTOL, "atol": ATOL, "learned_dt": False,
+                                   "reductions and error norm; learned step-size proposer "
+                                   "(DOPRI853 accepts/rejects every try)",
+                       "grid": N_GRID, "rtol": RTOL, "atol": ATOL, "learned_dt": True,
+                       "settle_t": 0.1,
                        "l2": "inputs larger than L2 (state 1.1 GB)",
                        "dt_next": mixed["dt_next"], "t_reached": mixed["t"],
                        "device_GB": mixed["device_bytes"] / 1e9},
