@@ -142,8 +142,13 @@ class Clocks:
                 "samples": len(sm)}
 
 
+ENGINE_NAMES = {0: "stockham", 1: "two-step", 2: "two-step-half"}
+
+
 def make_context(gpu, precision, device):
-    ctx = gpu.Context(n=(N_GRID,) * 3, L=(L_BOX,) * 3, precision=precision, device=device)
+    # the FFT engines are autotuned on the device when the context is made
+    ctx = gpu.Context(n=(N_GRID,) * 3, L=(L_BOX,) * 3, precision=precision, device=device,
+                      autotune=True)
     return ctx
 
 
@@ -191,7 +196,9 @@ def bench_form(gpu, precision, device, seed, steps, warmup, profile=False, clock
     if profile:
         ctx.profile(False)
     res = {"ms": ms, "mt": mt, "dt_next": dt, "launches": launches, "kernels": kern, "clocks": clk,
-           "t": ctx.t, "device_bytes": ctx.device_bytes}
+           "t": ctx.t, "device_bytes": ctx.device_bytes,
+           "fft_engines": dict(zip(("x", "y", "deriv4_x"),
+                                   (ENGINE_NAMES[e] for e in ctx.engines())))}
     return ctx, res
 
 
@@ -337,7 +344,8 @@ def main():
                        "settle_t": 0.1,
                        "l2": "inputs larger than L2 (state 1.1 GB)",
                        "dt_next": mixed["dt_next"], "t_reached": mixed["t"],
-                       "device_GB": mixed["device_bytes"] / 1e9},
+                       "device_GB": mixed["device_bytes"] / 1e9,
+                       "fft_engines": mixed["fft_engines"]},
             "gpu_launches": mixed["launches"],
             "e2e": {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")}
                    | {"value": e2e_val},

@@ -49,7 +49,8 @@ enum { IH_PREC_F64 = 0, IH_PREC_MIXED = 1 };
 
 /* Grid and physics parameters: the parameters.sh keys of the hot path. */
 typedef struct {
-    int nx, ny, nz;        /* GRIDPOINTS_X/Y/Z: powers of two, nx >= ny >= nz >= 4 */
+    int nx, ny, nz;        /* GRIDPOINTS_X/Y/Z: powers of two, nx >= ny >= nz >= 8,
+                              nx <= 256 (FP64) or 512 (mixed form) */
     double lx, ly, lz;     /* SPATIAL_UPPER_BOUND_* - SPATIAL_LOWER_BOUND_* */
     double mass;           /* MASS (V = m^2 phi^2 / 2) */
     int enable_gw;         /* ENABLE_GW */
@@ -129,7 +130,8 @@ int ih_mk_rhs_dev(ih_context *c, double t, double *f_dev, double *result_dev,
 /* <rho>, <p> of the last RHS (the reference's rho_mean, pressure_mean). */
 int ih_get_means(const ih_context *c, double *rho_mean, double *pressure_mean);
 /* Copy a per-point field of the last RHS to host (N doubles):
- * which = 0 rho, 1 pressure, 2 laplacian of phi, 3 squared gradient. */
+ * which = 0 rho, 1 pressure, 2 laplacian of phi (3, the squared gradient, is
+ * not kept by the fused RHS pass and returns IH_ERR_ARG). */
 int ih_get_field(ih_context *c, int which, double *out_host);
 int ih_get_output(ih_context *c, ih_output *out);
 /* prepare_and_save_timeslice without save() (toolbox.c:96-104): the RHS of
@@ -159,6 +161,31 @@ int ih_mean_dev(ih_context *c, const double *f_dev, size_t n, double *out_dev);
 int ih_mean_dev_noalloc(const double *f_dev, size_t n, double *out_dev, void *stream);
 size_t ih_mean_dev_noalloc_max_n(void);
 
+/* mean and variance (toolbox.c:726-734, 744-754) of n doubles in HOST memory,
+ * computed on the device (copied into the context's staging buffer, FP64 block
+ * sums): variance = (sum (f-mean)^2 - (sum (f-mean))^2 / n) / (n - 1) around
+ * the caller's mean, as the reference computes it.  n <= Ntot of the grid
+ * (IH_ERR_TOO_LARGE otherwise). */
+int ih_mean_host(ih_context *c, const double *f_host, size_t n, double *out);
+int ih_variance_host(ih_context *c, double mean, const double *f_host, size_t n,
+                     double *out);
+
+/* ---- FFT autotuner (no reference counterpart; FFTW's planner flag
+ * FFTW_DEFAULT_FLAG, parameters.sh, plays this role there) ----
+ * Times every engine variant of the x and y passes and of the fused inverse
+ * x pass of the RHS on the context's scratch spectra and keeps the fastest
+ * per pass.  Until it is called the passes use the shared-memory Stockham
+ * engine.  Results are identical across variants up to rounding.  The report
+ * lists the timings and the choice (valid until the next ih_autotune). */
+int ih_autotune(ih_context *c);
+const char *ih_autotune_report(const ih_context *c);
+/* Pin or read the engine of one pass: pass 0 = x, 1 = y, 2 = the fused
+ * inverse x pass; engine IH_FFT_STOCKHAM, IH_FFT_TWOSTEP (register two-step,
+ * 128-byte tiles) or IH_FFT_TWOSTEP_HALF (64-byte tiles). */
+enum { IH_FFT_STOCKHAM = 0, IH_FFT_TWOSTEP = 1, IH_FFT_TWOSTEP_HALF = 2 };
+int ih_fft_set_engine(ih_context *c, int pass, int engine);
+int ih_fft_get_engine(const ih_context *c, int pass);
+
 /* ---- transforms (fft / ifft, toolbox.c:806-827) on host buffers ----
  * r2c unnormalised exp(-i..) [x][y][z/2+1]; c2r unnormalised exp(+i..).
  * Computed in the context's precision. */
@@ -182,6 +209,11 @@ int ih_initial_psi(ih_context *c);
  * toolbox.c:96-104). */
 int ih_dopri853_init(ih_context *c, const ih_dopri_cfg *cfg, double t0,
                      double dt0);
+/* The same with the output flag of that first RHS selectable: run_dopri853
+ * opens with prepare_and_save_timeslice (dopri853.c:115, toolbox.c:96-104),
+ * whose filtered RHS also computes the diagnostics (want_output = 1). */
+int ih_dopri853_init_ex(ih_context *c, const ih_dopri_cfg *cfg, double t0,
+                        double dt0, int want_output);
 /* perform_step with dt_try; want_output=1 computes the diagnostics on the
  * post-step RHS (dopri853.c:288-291). */
 int ih_dopri853_step(ih_context *c, double dt_try, int want_output,
@@ -239,6 +271,11 @@ int ih_dopri853_set_proposer(ih_context *c, ih_mlp *m);
 /* One step of size dt from the context time; the stage-1 RHS runs with
  * filter=1 and, if want_output, output=1 (rk4.c:63-75). */
 int ih_rk4_step(ih_context *c, double dt, int want_output);
+/* The state at the start of the last RK4 or DOPRI853 step as that step used
+ * it (after its filter): what rk4.c's save() reads from field at an output
+ * step (rk4.c:66-72), in the reference layout (Ntot doubles).  No reference
+ * counterpart (the reference's field array is that state at that moment). */
+int ih_get_step_start_state(ih_context *c, double *f_host);
 
 /* Mixed form only: before an element of the two embedded error vectors enters
  * the FP64 error norm, its FP32 rounding floor eta * 2^-24 * sum_j |c_j k_j|

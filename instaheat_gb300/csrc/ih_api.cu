@@ -67,10 +67,10 @@ static int validate(const ih_params *p, std::string *why) {
     *why = "the 3D GPU path needs nz >= 8";
     return IH_ERR_ARG;
   }
-  const int zmax = p->precision == IH_PREC_MIXED ? 512 : 256;
-  if (p->nx > 512 || p->nz > zmax) {
-    *why = "grid too large for the shared-memory FFT tiles (nx <= 512; nz <= 256 in FP64, "
-           "<= 512 in the mixed form)";
+  const int nmax = p->precision == IH_PREC_MIXED ? 512 : 256;
+  if (p->nx > nmax || p->nz > nmax) {
+    *why = "grid too large for the FFT tiles (every axis <= 256 in FP64, <= 512 in the mixed "
+           "form)";
     return IH_ERR_ARG;
   }
   if (!(p->lx > 0 && p->ly > 0 && p->lz > 0)) {
@@ -303,6 +303,7 @@ int ih_set_state(ih_context *h, const double *f, double t) {
   IH_TRY(vec_from_ref(c, (const double *)c->stage_dev, c->y));
   c->t = t;
   c->have_state = 1;
+  c->step_start_valid = 0;
   IH_CUDA(c, cudaStreamSynchronize(c->stream));
   return IH_OK;
 }
@@ -312,6 +313,18 @@ int ih_get_state(ih_context *h, double *f) {
   if (!f) return IH_ERR_ARG;
   Ctx *c = &h->c;
   IH_TRY(vec_to_ref(c, c->y, (double *)c->stage_dev));
+  return download_ref(c, f);
+}
+
+int ih_get_step_start_state(ih_context *h, double *f) {
+  CTX_CHECK(h);
+  if (!f) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  if (!c->step_start_valid) {
+    c->err = "no step since the last mk_rhs or state upload";
+    return IH_ERR_STATE;
+  }
+  IH_TRY(vec_to_ref(c, c->ynew, (double *)c->stage_dev));
   return download_ref(c, f);
 }
 
@@ -339,6 +352,7 @@ int ih_mk_rhs_dev(ih_context *h, double t, double *f_dev, double *result_dev, in
   if (!f_dev || !result_dev) return IH_ERR_ARG;
   Ctx *c = &h->c;
   IH_TRY(vec_from_ref(c, f_dev, c->ytmp));
+  c->step_start_valid = 0;
   IH_TRY(rhs(c, t, c->ytmp, c->ynew, filter, output, nullptr));
   if (filter == 1 && c->p.enable_filter) IH_TRY(vec_to_ref(c, c->ytmp, f_dev));
   const Geom &g = c->g;
@@ -363,6 +377,7 @@ int ih_mk_rhs_host(ih_context *h, double t, double *f, double *result, int filte
   const Geom &g = c->g;
   IH_TRY(upload_ref(c, f));
   IH_TRY(vec_from_ref(c, (const double *)c->stage_dev, c->ytmp));
+  c->step_start_valid = 0;
   IH_TRY(rhs(c, t, c->ytmp, c->ynew, filter, output, nullptr));
   if (filter == 1 && c->p.enable_filter) {
     IH_TRY(vec_to_ref(c, c->ytmp, (double *)c->stage_dev));
@@ -414,6 +429,67 @@ int ih_mean_dev(ih_context *h, const double *f_dev, size_t n, double *out_dev) {
   IH_TRY(reduce_mean_f64(c, f_dev, (long long)n, out_dev));
   IH_CUDA(c, cudaStreamSynchronize(c->stream));
   return IH_OK;
+}
+
+// mean / variance of a host array on the device; the results pass through
+// diag slots 112-113
+static int host_stats(ih_context *h, const double *f, size_t n, int var, double mean,
+                      double *out) {
+  CTX_CHECK(h);
+  if (!f || !out || n == 0 || (var && n < 2)) return IH_ERR_ARG;
+  Ctx *c = &h->c;
+  if (n > c->g.Ntot) {
+    c->err = "array longer than the staging buffer (Ntot doubles)";
+    return IH_ERR_TOO_LARGE;
+  }
+  double *d = c->diag + 4 * c->g.bins + 112;
+  IH_CUDA(c, cudaMemcpyAsync(c->stage_dev, f, sizeof(double) * n, cudaMemcpyHostToDevice,
+                             c->stream));
+  if (var) {
+    IH_TRY(variance_f64(c, (const double *)c->stage_dev, (long long)n, mean, d));
+  } else {
+    IH_TRY(reduce_mean_f64(c, (const double *)c->stage_dev, (long long)n, d));
+  }
+  IH_CUDA(c, cudaMemcpyAsync(c->hpin, d, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  *out = var ? c->hpin[1] : c->hpin[0];
+  return IH_OK;
+}
+
+int ih_mean_host(ih_context *h, const double *f_host, size_t n, double *out) {
+  return host_stats(h, f_host, n, 0, 0.0, out);
+}
+
+int ih_variance_host(ih_context *h, double mean, const double *f_host, size_t n, double *out) {
+  return host_stats(h, f_host, n, 1, mean, out);
+}
+
+int ih_autotune(ih_context *h) {
+  CTX_CHECK(h);
+  Ctx *c = &h->c;
+  IH_TRY(fft_autotune(c));
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IH_OK;
+}
+
+const char *ih_autotune_report(const ih_context *h) {
+  return h ? h->c.tune_report.c_str() : "";
+}
+
+int ih_fft_set_engine(ih_context *h, int pass, int engine) {
+  CTX_CHECK(h);
+  if (pass < 0 || pass > 2 || engine < 0 || engine >= FV_COUNT) return IH_ERR_ARG;
+  if (pass < 2) {
+    h->c.xy_var[pass] = engine;
+  } else {
+    h->c.d4_var = engine;
+  }
+  return IH_OK;
+}
+
+int ih_fft_get_engine(const ih_context *h, int pass) {
+  if (!h || pass < 0 || pass > 2) return -1;
+  return pass < 2 ? h->c.xy_var[pass] : h->c.d4_var;
 }
 
 int ih_fft_host(ih_context *h, const double *in, double *out_c) {
@@ -470,6 +546,11 @@ int ih_initial_psi(ih_context *h) {
 }
 
 int ih_dopri853_init(ih_context *h, const ih_dopri_cfg *cfg, double t0, double dt0) {
+  return ih_dopri853_init_ex(h, cfg, t0, dt0, 0);
+}
+
+int ih_dopri853_init_ex(ih_context *h, const ih_dopri_cfg *cfg, double t0, double dt0,
+                        int want_output) {
   CTX_CHECK(h);
   if (!cfg || !(cfg->rtol >= 0) || !(cfg->atol >= 0) || !(dt0 > 0)) return IH_ERR_ARG;
   Ctx *c = &h->c;
@@ -477,7 +558,7 @@ int ih_dopri853_init(ih_context *h, const ih_dopri_cfg *cfg, double t0, double d
     c->err = "no state";
     return IH_ERR_STATE;
   }
-  IH_TRY(dopri_init(c, cfg, t0, dt0));
+  IH_TRY(dopri_init(c, cfg, t0, dt0, want_output ? 1 : 0));
   IH_CUDA(c, cudaStreamSynchronize(c->stream));
   return IH_OK;
 }

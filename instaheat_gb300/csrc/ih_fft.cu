@@ -5,17 +5,21 @@
 // exp(-2 pi i jk/n) transform into the half spectrum [nx][ny][nz/2+1], c2r the
 // unnormalised exp(+2 pi i jk/n) inverse.
 //
-// Structure: three passes per transform, each a kernel that stages a tile of
-// pencils in shared memory and runs an in-place radix-4 (+2) Stockham FFT on
-// it.  Tiles are [L][B+1] complex (pencil index innermost, one pad column
-// against bank conflicts).  In the x and y passes B is one 128-byte line of
-// complex values (16 for FP32, 8 for FP64), so every global row access is a
-// full line; the z passes read whole contiguous rows, so their B (rows per
-// CTA) is chosen for occupancy.  Lengths and tile widths are powers of two and
-// all index arithmetic is shifts and masks.  The z pass treats a real row of
-// length nz as nz/2 complex values and applies the even/odd split.  Twiddles
-// come from tables computed once in FP64 on the host (exp(-2 pi i k/L)) and
-// staged into shared memory.
+// Structure: three passes per transform (z, y, x), each one kernel.  Every
+// pencil of length L = R1*R2 is transformed in two register steps with one
+// shared-memory exchange:
+//   step 1: thread (pencil, n1) holds x[n1 + R1*n2], n2 < R2, does an
+//           in-register R2-point DFT and multiplies by exp(-+2 pi i n1 k2/L);
+//   step 2: thread (pencil, k2) gathers the R1 values of its k2, does an
+//           in-register R1-point DFT and owns X[k2 + R2*k1].
+// The in-register DFTs are radix-2 decimation-in-frequency networks whose
+// loop structure and bit reversal are resolved at compile time; their
+// twiddles come from a table exp(-2 pi i m/L) computed once in FP64 on the
+// host and staged in shared memory.  x and y passes load straight from global
+// memory into registers (tiles of B pencils, B = one 128-byte line of complex
+// values: 16 FP32 / 8 FP64) and store straight back.  z passes work on whole
+// contiguous rows (a real row of nz values packed as nz/2 complex, with the
+// even/odd split) and stage the rows in shared memory for the split.
 //
 // Fused passes (the RHS never materialises ik*phihat or the six real
 // products d_i phi d_j phi):
@@ -62,12 +66,66 @@ __device__ __forceinline__ V csub(V a, V b) {
 
 template <typename T> __host__ __device__ constexpr int tileB() { return 128 / (int)(2 * sizeof(T)); }
 __host__ __device__ constexpr int clog2(int v) { return v <= 1 ? 0 : 1 + clog2(v >> 1); }
-static int ilog2(int v) {
-  int l = 0;
-  while ((1 << l) < v) ++l;
-  return l;
+__host__ __device__ constexpr int brev(int x, int bits) {
+  return bits == 0 ? 0 : (((x & 1) << (bits - 1)) | brev(x >> 1, bits - 1));
 }
 
+// L = R1 * R2: threads per pencil in step 1, points per thread in step 1
+template <int L> struct Fac;
+template <> struct Fac<4> { static constexpr int R1 = 2, R2 = 2; };
+template <> struct Fac<8> { static constexpr int R1 = 4, R2 = 2; };
+template <> struct Fac<16> { static constexpr int R1 = 4, R2 = 4; };
+template <> struct Fac<32> { static constexpr int R1 = 8, R2 = 4; };
+template <> struct Fac<64> { static constexpr int R1 = 8, R2 = 8; };
+template <> struct Fac<128> { static constexpr int R1 = 16, R2 = 8; };
+template <> struct Fac<256> { static constexpr int R1 = 16, R2 = 16; };
+template <> struct Fac<512> { static constexpr int R1 = 16, R2 = 32; };
+
+template <int L> __host__ __device__ constexpr int max_r() {
+  return Fac<L>::R1 > Fac<L>::R2 ? Fac<L>::R1 : Fac<L>::R2;
+}
+__host__ __device__ constexpr int round_warp(int n) { return n < 32 ? 32 : (n + 31) / 32 * 32; }
+// threads of a pass over B pencils (rows) of length L: one per pencil and
+// register column of the wider step
+template <int L, int B> __host__ __device__ constexpr int pass_threads() {
+  return round_warp(max_r<L>() * B);
+}
+// In-register DFT of R points: v[k] <- sum_n v[n] exp(sign 2 pi i nk/R).
+// tw[m * ts] = exp(-2 pi i m/R).  Radix-2 decimation in frequency; the
+// bit-reversed result order is undone by a compile-time register permutation.
+template <typename T, int R>
+__device__ __forceinline__ void reg_dft(C2<T> (&v)[R], const C2<T> *tw, int ts, int sign) {
+  constexpr int LOGR = clog2(R);
+#pragma unroll
+  for (int s = 0; s < LOGR; ++s) {
+    const int len = R >> s, half = len >> 1;
+#pragma unroll
+    for (int st = 0; st < R; st += len) {
+#pragma unroll
+      for (int j = 0; j < half; ++j) {
+        const C2<T> a = v[st + j], b = v[st + j + half];
+        v[st + j] = cadd(a, b);
+        const C2<T> d = csub(a, b);
+        if (j == 0) {
+          v[st + j + half] = d;
+        } else if (4 * j == len) {  // exp(sign i pi/2) = sign * i
+          v[st + j + half] = mk2<T>(-(T)sign * d.y, (T)sign * d.x);
+        } else {
+          C2<T> w = tw[j * (R / len) * ts];
+          if (sign > 0) w.y = -w.y;
+          v[st + j + half] = cmul(d, w);
+        }
+      }
+    }
+  }
+  C2<T> t[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) t[k] = v[brev(k, LOGR)];
+#pragma unroll
+  for (int k = 0; k < R; ++k) v[k] = t[k];
+}
+
+// exp(sign 2 pi i m / L) from the table exp(-2 pi i m/L)
 // Butterflies per thread per radix-4 stage (2K per radix-2 stage); the
 // launchers size CTAs so that B*L <= 4*K*nt.
 constexpr int kFftK = 2;
@@ -170,16 +228,30 @@ __device__ void smem_fft(C2<T> *s, int L, int P, const C2<T> *tw, int sign, int 
 }
 
 template <typename V>
+__device__ __forceinline__ V twid(const V *tw, int m, int sign) {
+  V w = tw[m];
+  if (sign > 0) w.y = -w.y;
+  return w;
+}
+
+template <typename V>
 __device__ __forceinline__ void load_table(V *dst, const V *src, int n, int tid, int nt) {
   for (int i = tid; i < n; i += nt) dst[i] = src[i];
 }
 
 // ---------------------------------------------------------------------------
-// complex pass along x (axis 0) or y (axis 1), in place, batched over arrays
-template <typename T>
-__global__ void k_fft_xy(C2<T> *data, long long astride, int L, long long sj,
-                         long long so, int mz, int sign, const C2<T> *twg) {
-  constexpr int B = tileB<T>();
+// Complex passes along x (axis 0) or y (axis 1), in place, batched over
+// arrays (blockIdx.z).  A CTA transforms a tile of B pencils: columns
+// z0..z0+B-1 of one plane, element j of a pencil at j * sj.  Two engines,
+// chosen per axis by the autotuner (fft_autotune):
+//   Stockham  -- the tile is staged in shared memory [L][B+1] and transformed
+//                in place by radix-4/2 Stockham stages (smem_fft);
+//   two-step  -- L = R1 R2: each thread loads R2 elements straight into
+//                registers, runs an R2-point DFT and one twiddle, exchanges
+//                through shared memory once, runs an R1-point DFT and stores.
+template <typename T, int B>
+__global__ void k_fft_xy_st(C2<T> *data, long long astride, int L, long long sj,
+                            long long so, int mz, int sign, const C2<T> *twg) {
   constexpr int P = B + 1;
   constexpr int LB = clog2(B);
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -202,47 +274,181 @@ __global__ void k_fft_xy(C2<T> *data, long long astride, int L, long long sj,
   }
 }
 
-// post-processing of one forward half-length row: X_k = E_k + w^k O_k
-template <typename T>
-__device__ __forceinline__ C2<T> zr2c_post(const C2<T> *s, int k, int h, int P, int b,
-                                           const C2<T> *wz) {
-  C2<T> z = s[(k & (h - 1)) * P + b], zc = s[((h - k) & (h - 1)) * P + b];
-  zc.y = -zc.y;
-  C2<T> e = mk2<T>((T)0.5 * (z.x + zc.x), (T)0.5 * (z.y + zc.y));
-  // O = (Z - conj Z_{h-k}) / (2i)
-  C2<T> o = mk2<T>((T)0.5 * (z.y - zc.y), -(T)0.5 * (z.x - zc.x));
-  return cadd(e, cmul(o, wz[k]));
-}
-
-// forward real-to-complex pass along z: BZ rows of nz reals -> nz/2+1 complex
-template <typename T, int BZ>
-__global__ void k_fft_zr2c(const T *in, long long istride, C2<T> *out, long long ostride,
-                           long long rows, int h, int logh, const C2<T> *twh,
-                           const C2<T> *twz) {
-  constexpr int P = BZ + 1;
+template <typename T, int L, int B>
+__global__ void __launch_bounds__(pass_threads<L, B>()) k_fft_xy_2s(C2<T> *data, long long astride, long long sj, long long so, int mz,
+                         int sign, const C2<T> *twg) {
+  constexpr int R1 = Fac<L>::R1, R2 = Fac<L>::R2;
+  constexpr int LB = clog2(B), P = B + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   C2<T> *tw = reinterpret_cast<C2<T> *>(smraw);
-  C2<T> *wz = tw + h;
-  C2<T> *s = wz + h + 1;
+  C2<T> *x1 = tw + L;  // [n1*R2 + k2][P]
   const int tid = threadIdx.x, nt = blockDim.x;
-  const int mz = h + 1;
-  const long long r0 = (long long)blockIdx.x * BZ;
-  const int bv = (int)min((long long)BZ, rows - r0);
-  const C2<T> *src = reinterpret_cast<const C2<T> *>(in + blockIdx.z * istride) + r0 * h;
-  C2<T> *dst = out + blockIdx.z * ostride + r0 * mz;
-  load_table(tw, twh, h, tid, nt);
-  load_table(wz, twz, h + 1, tid, nt);
-  for (int idx = tid; idx < BZ * h; idx += nt) {
-    const int b = idx >> logh, j = idx & (h - 1);
-    s[j * P + b] = (b < bv) ? src[(long long)b * h + j] : mk2<T>(0, 0);
+  const int z0 = blockIdx.x * B;
+  const int bv = min(B, mz - z0);
+  C2<T> *base = data + blockIdx.z * astride + (long long)blockIdx.y * so + z0;
+  load_table(tw, twg, L, tid, nt);
+  __syncthreads();
+  if (tid < R1 * B) {
+    const int b = tid & (B - 1), n1 = tid >> LB;
+    C2<T> v[R2];
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2)
+      v[n2] = (b < bv) ? base[(long long)(n1 + R1 * n2) * sj + b] : mk2<T>(0, 0);
+    reg_dft<T, R2>(v, tw, L / R2, sign);
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2)
+      x1[(n1 * R2 + k2) * P + b] = (k2 == 0) ? v[k2] : cmul(v[k2], twid(tw, (n1 * k2) & (L - 1), sign));
   }
   __syncthreads();
-  smem_fft<T, BZ, kFftK>(s, h, P, tw, -1, tid, nt);
-  for (int b = 0; b < bv; ++b)
-    for (int k = tid; k < mz; k += nt) dst[(long long)b * mz + k] = zr2c_post<T>(s, k, h, P, b, wz);
+  if (tid < R2 * B) {
+    const int b = tid & (B - 1), k2 = tid >> LB;
+    C2<T> u[R1];
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) u[n1] = x1[(n1 * R2 + k2) * P + b];
+    reg_dft<T, R1>(u, tw, L / R1, sign);
+    if (b < bv) {
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) base[(long long)(k2 + R2 * k1) * sj + b] = u[k1];
+    }
+  }
 }
 
-// z pre-processing of one half-spectrum row into the packed complex row
+// ---------------------------------------------------------------------------
+// z passes.  A row of H = nz/2 complex values (the real row packed as
+// z_j = x_2j + i x_2j+1) belongs to a group of W = min(32, H) lanes of one
+// warp; each lane holds R = H/W values in one of two index maps:
+//   natural   -- lane t, register n holds element t + W n;
+//   scrambled -- lane t, register k1 holds element k1 + R brev(t).
+// Forward (decimation in frequency): natural in, R-point DFT in registers,
+// twiddle w_H^(t k1), W-point DFT across the lanes by shuffles, scrambled out.
+// Inverse (decimation in time): the mirror image, scrambled in, natural out.
+// Inverse passes load their scrambled input straight from global memory (a
+// row is 1-2 KB and stays in L1), so they use no shared memory; forward
+// passes stage their scrambled output through a per-warp shared row so that
+// whole lines are stored.
+template <int H> struct ZGeo {
+  static constexpr int W = H < 32 ? H : 32;
+  static constexpr int R = H / W;
+  static constexpr int LW = clog2(W);
+  static constexpr int LR = clog2(R);
+  static constexpr int G = 32 / W;  // rows per warp
+  // staging row: H+1 values, one pad slot after every R (breaks the stride-R
+  // bank pattern of the scrambled writes)
+  static constexpr int PS = R > 1 ? H + H / R + 1 : H + 1;
+  __device__ static __forceinline__ int pad(int k) { return R > 1 ? k + (k >> LR) : k; }
+};
+
+__device__ __forceinline__ int lane_brev(int t, int lw) {
+  return (int)(__brev((unsigned)t) >> (32 - lw));
+}
+
+// conjugate for the inverse direction (S = +1)
+template <int S, typename V>
+__device__ __forceinline__ V cj(V w) {
+  if (S > 0) w.y = -w.y;
+  return w;
+}
+template <typename V>
+__device__ __forceinline__ V shfl_xor_c(V v, int m) {
+  v.x = __shfl_xor_sync(0xffffffffu, v.x, m);
+  v.y = __shfl_xor_sync(0xffffffffu, v.y, m);
+  return v;
+}
+template <typename V>
+__device__ __forceinline__ V shfl_idx_c(V v, int src) {
+  v.x = __shfl_sync(0xffffffffu, v.x, src);
+  v.y = __shfl_sync(0xffffffffu, v.y, src);
+  return v;
+}
+
+// per-lane twiddles of the forward transform (the inverse conjugates them)
+template <typename T, int H> struct ZTw {
+  using Gm = ZGeo<H>;
+  C2<T> st[Gm::LW];  // stage q (half-span 2^q): w_(2^(q+1))^(t mod 2^q) on upper lanes, 1 on lower
+  T sg[Gm::LW];      // +1 on the lower, -1 on the upper lane of stage q
+  C2<T> ta[Gm::R];   // w_H^(t k1)
+  __device__ __forceinline__ void load(const C2<T> *__restrict__ twh, int t) {
+#pragma unroll
+    for (int q = 0; q < Gm::LW; ++q) {
+      const int m = 1 << q;
+      const bool up = (t & m) != 0;
+      sg[q] = up ? (T)-1 : (T)1;
+      st[q] = up ? twh[(t & (m - 1)) * (H / (2 * m))] : mk2<T>(1, 0);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < Gm::R; ++k1) ta[k1] = twh[t * k1];
+  }
+};
+
+// natural -> scrambled, sign S
+template <int S, typename T, int H>
+__device__ __forceinline__ void zfft_dif(C2<T> (&v)[ZGeo<H>::R], const ZTw<T, H> &w,
+                                         const C2<T> *__restrict__ twh) {
+  using Gm = ZGeo<H>;
+  reg_dft<T, Gm::R>(v, twh, H / Gm::R, S);
+#pragma unroll
+  for (int k1 = 1; k1 < Gm::R; ++k1) v[k1] = cmul(v[k1], cj<S>(w.ta[k1]));
+#pragma unroll
+  for (int q = Gm::LW - 1; q >= 0; --q) {
+#pragma unroll
+    for (int r = 0; r < Gm::R; ++r) {
+      const C2<T> p = shfl_xor_c(v[r], 1 << q);
+      // lower lane: v + p; upper lane: (p - v) * twiddle
+      const C2<T> d = mk2<T>(fma(w.sg[q], v[r].x, p.x), fma(w.sg[q], v[r].y, p.y));
+      v[r] = (q == 0) ? d : cmul(d, cj<S>(w.st[q]));
+    }
+  }
+}
+
+// scrambled -> natural, sign S
+template <int S, typename T, int H>
+__device__ __forceinline__ void zfft_dit(C2<T> (&v)[ZGeo<H>::R], const ZTw<T, H> &w,
+                                         const C2<T> *__restrict__ twh) {
+  using Gm = ZGeo<H>;
+#pragma unroll
+  for (int q = 0; q < Gm::LW; ++q) {
+#pragma unroll
+    for (int r = 0; r < Gm::R; ++r) {
+      if (q > 0) v[r] = cmul(v[r], cj<S>(w.st[q]));  // upper lane: twiddle first
+      const C2<T> p = shfl_xor_c(v[r], 1 << q);
+      // lower lane: v + p; upper lane: p - v
+      v[r] = mk2<T>(fma(w.sg[q], v[r].x, p.x), fma(w.sg[q], v[r].y, p.y));
+    }
+  }
+#pragma unroll
+  for (int k1 = 1; k1 < Gm::R; ++k1) v[k1] = cmul(v[k1], cj<S>(w.ta[k1]));
+  reg_dft<T, Gm::R>(v, twh, H / Gm::R, S);
+}
+
+// r2c post-processing of a forward-transformed row held scrambled:
+// X_k = E_k + exp(-2 pi i k/nz) O_k with E_k = (Z_k + conj Z_(H-k))/2 and
+// O_k = (Z_k - conj Z_(H-k))/(2i).  v[k1] = Z_k on entry, X_k on return
+// (k = k1 + R brev(t)); xH = X_H, valid on the lane with t == 0.  The partner
+// Z_(H-k) of register k1 > 0 sits in register R-k1 of lane t^(W-1); that of
+// register 0 in register 0 of lane brev((W - brev(t)) mod W).
+template <typename T, int H>
+__device__ __forceinline__ void zr2c_post_lanes(C2<T> (&v)[ZGeo<H>::R], int t, int gbase,
+                                                const C2<T> *__restrict__ twz, C2<T> &xH) {
+  using Gm = ZGeo<H>;
+  const int b = lane_brev(t, Gm::LW);
+  C2<T> pz[Gm::R];
+  pz[0] = shfl_idx_c(v[0], gbase + lane_brev((Gm::W - b) & (Gm::W - 1), Gm::LW));
+#pragma unroll
+  for (int k1 = 1; k1 < Gm::R; ++k1) pz[k1] = shfl_xor_c(v[Gm::R - k1], Gm::W - 1);
+#pragma unroll
+  for (int k1 = 0; k1 < Gm::R; ++k1) {
+    const C2<T> z = v[k1];
+    const C2<T> zc = mk2<T>(pz[k1].x, -pz[k1].y);
+    const C2<T> e = mk2<T>((T)0.5 * (z.x + zc.x), (T)0.5 * (z.y + zc.y));
+    const C2<T> o = mk2<T>((T)0.5 * (z.y - zc.y), -(T)0.5 * (z.x - zc.x));
+    if (k1 == 0) xH = csub(e, o);  // exp(-i pi) = -1
+    v[k1] = cadd(e, cmul(o, twz[k1 + Gm::R * b]));
+  }
+}
+
+// c2r pre-processing of half-spectrum element k into the packed row:
+// Z_k = E_k + i O_k, E_k = X_k + conj X_(H-k),
+// O_k = (X_k - conj X_(H-k)) exp(+2 pi i k/nz)
 template <typename T>
 __device__ __forceinline__ C2<T> zc2r_pre(const C2<T> *row, int k, int h, const C2<T> *wz) {
   C2<T> x = row[k], xc = row[h - k];
@@ -254,34 +460,75 @@ __device__ __forceinline__ C2<T> zc2r_pre(const C2<T> *row, int k, int h, const 
   return mk2<T>(e.x - o.y, e.y + o.x);  // E + i O
 }
 
-// inverse complex-to-real pass along z
-template <typename T, int BZ>
-__global__ void k_fft_zc2r(const C2<T> *in, long long istride, T *out, long long ostride,
-                           long long rows, int h, int logh, const C2<T> *twh,
-                           const C2<T> *twz) {
-  constexpr int P = BZ + 1;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  C2<T> *tw = reinterpret_cast<C2<T> *>(smraw);
-  C2<T> *wz = tw + h;
-  C2<T> *s = wz + h + 1;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int mz = h + 1;
-  const long long r0 = (long long)blockIdx.x * BZ;
-  const int bv = (int)min((long long)BZ, rows - r0);
-  const C2<T> *src = in + blockIdx.z * istride + r0 * mz;
-  C2<T> *dst = reinterpret_cast<C2<T> *>(out + blockIdx.z * ostride) + r0 * h;
-  load_table(tw, twh, h, tid, nt);
-  load_table(wz, twz, h + 1, tid, nt);
-  __syncthreads();
-  for (int idx = tid; idx < BZ * h; idx += nt) {
-    const int b = idx >> logh, k = idx & (h - 1);
-    s[k * P + b] = (b < bv) ? zc2r_pre<T>(src + (long long)b * mz, k, h, wz) : mk2<T>(0, 0);
+// store a scrambled r2c row (H+1 values) as whole lines through the warp's
+// staging row
+template <typename T, int H>
+__device__ __forceinline__ void zstore_row(const C2<T> (&v)[ZGeo<H>::R], C2<T> xH, int t,
+                                           C2<T> *srow, C2<T> *dst, bool valid) {
+  using Gm = ZGeo<H>;
+  const int b = lane_brev(t, Gm::LW);
+#pragma unroll
+  for (int k1 = 0; k1 < Gm::R; ++k1) srow[Gm::pad(k1 + Gm::R * b)] = v[k1];
+  if (t == 0) srow[Gm::pad(H)] = xH;
+  __syncwarp();
+  if (valid) {
+#pragma unroll
+    for (int n = 0; n < Gm::R; ++n) dst[t + Gm::W * n] = srow[Gm::pad(t + Gm::W * n)];
+    if (t == 0) dst[H] = srow[Gm::pad(H)];
   }
-  __syncthreads();
-  smem_fft<T, BZ, kFftK>(s, h, P, tw, +1, tid, nt);
-  for (int idx = tid; idx < BZ * h; idx += nt) {
-    const int b = idx >> logh, j = idx & (h - 1);
-    if (b < bv) dst[(long long)b * h + j] = s[j * P + b];
+  __syncwarp();
+}
+
+// warps per CTA of the z passes
+template <typename T> __host__ __device__ constexpr int zwarps() { return sizeof(T) == 4 ? 8 : 4; }
+
+// forward real-to-complex pass along z: rows of nz = 2H reals -> H+1 complex
+template <typename T, int H>
+__global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_zr2c(const T *in, long long istride, C2<T> *out, long long ostride,
+                           long long rows, const C2<T> *__restrict__ twh, const C2<T> *__restrict__ twz) {
+  using Gm = ZGeo<H>;
+  constexpr int WPB = zwarps<T>();
+  __shared__ C2<T> stage[WPB * Gm::G * Gm::PS];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int t = lane & (Gm::W - 1), gi = lane >> Gm::LW;
+  const long long row = ((long long)blockIdx.x * WPB + warp) * Gm::G + gi;
+  const bool valid = row < rows;
+  ZTw<T, H> w;
+  w.load(twh, t);
+  const C2<T> *src = reinterpret_cast<const C2<T> *>(in + blockIdx.y * istride) + row * H;
+  C2<T> v[Gm::R];
+#pragma unroll
+  for (int n = 0; n < Gm::R; ++n) v[n] = valid ? src[t + Gm::W * n] : mk2<T>(0, 0);
+  zfft_dif<-1, T, H>(v, w, twh);
+  C2<T> xH;
+  zr2c_post_lanes<T, H>(v, t, lane & ~(Gm::W - 1), twz, xH);
+  zstore_row<T, H>(v, xH, t, stage + (warp * Gm::G + gi) * Gm::PS,
+                   out + blockIdx.y * ostride + row * (H + 1), valid);
+}
+
+// inverse complex-to-real pass along z
+template <typename T, int H>
+__global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_zc2r(const C2<T> *in, long long istride, T *out, long long ostride,
+                           long long rows, const C2<T> *__restrict__ twh, const C2<T> *__restrict__ twz) {
+  using Gm = ZGeo<H>;
+  constexpr int WPB = zwarps<T>();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int t = lane & (Gm::W - 1), gi = lane >> Gm::LW;
+  const long long row = ((long long)blockIdx.x * WPB + warp) * Gm::G + gi;
+  const bool valid = row < rows;
+  ZTw<T, H> w;
+  w.load(twh, t);
+  const C2<T> *src = in + blockIdx.y * istride + row * (H + 1);
+  const int b = lane_brev(t, Gm::LW);
+  C2<T> v[Gm::R];
+#pragma unroll
+  for (int k1 = 0; k1 < Gm::R; ++k1)
+    v[k1] = valid ? zc2r_pre<T>(src, k1 + Gm::R * b, H, twz) : mk2<T>(0, 0);
+  zfft_dit<+1, T, H>(v, w, twh);
+  C2<T> *dst = reinterpret_cast<C2<T> *>(out + blockIdx.y * ostride) + row * H;
+  if (valid) {
+#pragma unroll
+    for (int n = 0; n < Gm::R; ++n) dst[t + Gm::W * n] = v[n];
   }
 }
 
@@ -314,10 +561,12 @@ __device__ __forceinline__ T ksq(const Geom &g, int ia, int ja, int kz) {
 // d/dx, d/dy, d/dz and laplacian spectra of phihat/N, inverse x transform each.
 // k vectors follow setup.c:609-666: first-derivative components are zero on
 // the Nyquist index, k^2 keeps it.
-template <typename T>
-__global__ void k_fft_x_deriv4_inv(const C2<T> *phihat, C2<T> *out, long long ostride, Geom g,
+// Two engines, as for the plain passes: Stockham (the phihat tile stays in
+// shared memory for the four variants) and two-step (each step-1 thread keeps
+// its R2 values of phihat in registers for the four variants).
+template <typename T, int B>
+__global__ void k_fft_x_deriv4_st(const C2<T> *phihat, C2<T> *out, long long ostride, Geom g,
                                    const C2<T> *twg) {
-  constexpr int B = tileB<T>();
   constexpr int P = B + 1;
   constexpr int LB = clog2(B);
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -372,177 +621,339 @@ __global__ void k_fft_x_deriv4_inv(const C2<T> *phihat, C2<T> *out, long long os
   }
 }
 
-// The fused last inverse z pass of the RHS (see the file comment).
-// Plain form (MIXED=false): the reference's expressions (toolbox.c:196-208,
-// 225-243) on full values.  Mixed form: homogeneous parts in FP64 scalars,
-// fluctuation parts in T:
-//   rho = rho_bar + drho,  rho_bar = (1/2 - psib) Pib^2 + m^2 phib^2 / 2,
-//   drho = (1/2 - psib)(2 Pib dPi + dPi^2) - dpsi (Pib + dPi)^2
-//          + (1/2 + psi) g / a^2 + m^2 phib dphi + m^2 dphi^2 / 2,
-// and likewise p; lap and p written as fluctuations.
-template <typename T, bool MIXED, int BZ>
-__global__ void k_fft_z_rhs_fused(const C2<T> *d4, long long dstride, const T *yfl,
-                                  const double *ysc, T *lap, T *pout, T *rhoout, C2<T> *s6,
-                                  long long sstride4, C2<T> *s6b, int gw, double *partials,
-                                  Geom g, int logh, const C2<T> *twh, const C2<T> *twz) {
-  constexpr int P = BZ + 1;
+// the two-step fused pass keeps phihat in registers: it asks the register
+// allocator for half the resident CTAs of a plain pass
+template <typename T, int L, int B> __host__ __device__ constexpr int d4_min_blocks() {
+  return (sizeof(T) == 4 ? 512 : 256) / pass_threads<L, B>() > 0
+             ? (sizeof(T) == 4 ? 512 : 256) / pass_threads<L, B>()
+             : 1;
+}
+
+template <typename T, int L, int B>
+__global__ void __launch_bounds__(pass_threads<L, B>(), (d4_min_blocks<T, L, B>())) k_fft_x_deriv4_2s(const C2<T> *phihat, C2<T> *out, long long ostride, Geom g,
+                                   const C2<T> *twg) {
+  constexpr int R1 = Fac<L>::R1, R2 = Fac<L>::R2;
+  constexpr int LB = clog2(B), P = B + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int h = g.h, mz = g.mz, nz = g.nz;
-  const int lognz = logh + 1;
   C2<T> *tw = reinterpret_cast<C2<T> *>(smraw);
-  C2<T> *wz = tw + h;
-  C2<T> *tile = wz + h + 1;  // 6 tiles of h*P
-  const int TS = h * P;
-  __shared__ double red[2][32];
+  C2<T> *x1 = tw + L;
   const int tid = threadIdx.x, nt = blockDim.x;
-  const long long rows = (long long)g.nx * g.ny;
-  const long long r0 = (long long)blockIdx.x * BZ;
-  const int bv = (int)min((long long)BZ, rows - r0);
-  load_table(tw, twh, h, tid, nt);
-  load_table(wz, twz, h + 1, tid, nt);
-  __syncthreads();
+  const int mz = g.mz;
+  const int z0 = blockIdx.x * B;
+  const int bv = min(B, mz - z0);
+  const int yj = blockIdx.y;
+  const long long sj = (long long)g.ny * mz;
+  const long long off = (long long)yj * mz + z0;
+  load_table(tw, twg, L, tid, nt);
+  const int ny = g.ny, nz = g.nz, nx = g.nx;
+  const T invN = (T)(1.0 / (double)g.N);
+  const T fy = (2 * yj == ny) ? (T)0 : kfac<T>(g.kyu, (yj > ny / 2) ? (yj - ny) : yj);
+  const int ja = (yj > ny / 2) ? (ny - yj) : yj;
+  // step-1 threads keep their R2 values of phihat/N in registers for all four
+  const bool s1 = tid < R1 * B;
+  const int b1 = tid & (B - 1), n1 = tid >> LB;
+  const int kz = z0 + b1;
+  const T fz = (2 * kz == nz) ? (T)0 : kfac<T>(g.kzu, kz);
+  C2<T> ph[R2];
+#pragma unroll
+  for (int n2 = 0; n2 < R2; ++n2) {
+    C2<T> v = (s1 && b1 < bv) ? phihat[off + (long long)(n1 + R1 * n2) * sj + b1] : mk2<T>(0, 0);
+    ph[n2] = mk2<T>(v.x * invN, v.y * invN);
+  }
   for (int a = 0; a < 4; ++a) {
-    const C2<T> *src = d4 + a * dstride + r0 * mz;
-    C2<T> *s = tile + a * TS;
-    for (int idx = tid; idx < BZ * h; idx += nt) {
-      const int b = idx >> logh, k = idx & (h - 1);
-      s[k * P + b] = (b < bv) ? zc2r_pre<T>(src + (long long)b * mz, k, h, wz) : mk2<T>(0, 0);
+    __syncthreads();
+    if (s1) {
+      C2<T> v[R2];
+#pragma unroll
+      for (int n2 = 0; n2 < R2; ++n2) {
+        const int i = n1 + R1 * n2;
+        const C2<T> pre = ph[n2];
+        T f;
+        if (a == 0) {
+          f = (2 * i == nx) ? (T)0 : kfac<T>(g.kxu, (i > nx / 2) ? (i - nx) : i);
+        } else if (a == 1) {
+          f = fy;
+        } else if (a == 2) {
+          f = fz;
+        } else {
+          f = ksq<T>(g, (i > nx / 2) ? (nx - i) : i, ja, kz);
+        }
+        v[n2] = (a < 3) ? mk2<T>(-pre.y * f, pre.x * f)    // pre * I * k
+                        : mk2<T>(-pre.x * f, -pre.y * f);  // -pre * k^2
+      }
+      reg_dft<T, R2>(v, tw, L / R2, +1);
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2)
+        x1[(n1 * R2 + k2) * P + b1] = (k2 == 0) ? v[k2] : cmul(v[k2], twid(tw, (n1 * k2) & (L - 1), +1));
+    }
+    __syncthreads();
+    if (tid < R2 * B) {
+      const int b = tid & (B - 1), k2 = tid >> LB;
+      C2<T> u[R1];
+#pragma unroll
+      for (int m1 = 0; m1 < R1; ++m1) u[m1] = x1[(m1 * R2 + k2) * P + b];
+      reg_dft<T, R1>(u, tw, L / R1, +1);
+      C2<T> *o = out + a * ostride + off;
+      if (b < bv) {
+#pragma unroll
+        for (int k1 = 0; k1 < R1; ++k1) o[(long long)(k2 + R2 * k1) * sj + b] = u[k1];
+      }
     }
   }
-  __syncthreads();
-  for (int a = 0; a < 4; ++a) smem_fft<T, BZ, kFftK>(tile + a * TS, h, P, tw, +1, tid, nt);
-  // pointwise
+}
+
+// energy density and pressure at one point (see above)
+template <typename T, bool MIXED>
+__device__ __forceinline__ void rho_p(T dx, T dy, T dz, T phi, T dph, T ps, T inv_a2, T m2, T third,
+                                      T phib, T pib, T psib, T &rho, T &p) {
+  T grad = dx * dx;
+  grad += dy * dy;
+  grad += dz * dz;
+  if (!MIXED) {
+    T t1 = ((T)0.5 - ps) * dph * dph;
+    T t2 = ((T)0.5 + ps) * grad * inv_a2;
+    T V = m2 * phi * phi * (T)0.5;
+    rho = t1 + t2 + V;
+    p = t1 - t2 * third - V;
+  } else {
+    T pif = pib + dph;
+    T kin = ((T)0.5 - psib) * ((T)2.0 * pib * dph + dph * dph) - ps * pif * pif;
+    T grd = ((T)0.5 + psib + ps) * grad * inv_a2;
+    T pot = m2 * phib * phi + (T)0.5 * m2 * phi * phi;
+    rho = kin + grd + pot;
+    p = kin - grd * third - pot;
+  }
+}
+
+template <typename T, bool MIXED, int H>
+__global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_z_rhs_fused(const C2<T> *d4, long long dstride, const T *yfl,
+                                  const double *ysc, T *lap, T *pout, T *rhoout, C2<T> *s6,
+                                  long long sstride4, C2<T> *s6b, int gw, double *partials,
+                                  Geom g, const C2<T> *__restrict__ twh, const C2<T> *__restrict__ twz) {
+  using Gm = ZGeo<H>;
+  constexpr int WPB = zwarps<T>(), R = Gm::R, W = Gm::W;
+  __shared__ C2<T> stage[WPB * Gm::G * Gm::PS];
+  __shared__ double red[2][WPB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int t = lane & (W - 1), gi = lane >> Gm::LW;
+  const long long rows = (long long)g.nx * g.ny;
+  const long long row = ((long long)blockIdx.x * WPB + warp) * Gm::G + gi;
+  const bool valid = row < rows;
+  ZTw<T, H> w;
+  w.load(twh, t);
+  const int b = lane_brev(t, Gm::LW);
+  // the four inverse transforms: d/dx, d/dy, d/dz, laplacian of phi
+  C2<T> d[4][R];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const C2<T> *src = d4 + a * dstride + row * (H + 1);
+#pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) d[a][k1] = valid ? zc2r_pre<T>(src, k1 + R * b, H, twz) : mk2<T>(0, 0);
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) zfft_dit<+1, T, H>(d[a], w, twh);
+  // pointwise, natural map: register n holds reals 2j, 2j+1 of j = t + W n
   const long long N = g.N;
   const double a_sc = ysc[4];
   const T inv_a2 = (T)(1.0 / (a_sc * a_sc));
   const T m2 = (T)(g.mass * g.mass);
   const T third = (T)(1.0 / 3.0);
-  T srho = 0, sp = 0;  // per-thread partials (a few points), then FP64
-  T *tl = reinterpret_cast<T *>(tile);
-  for (int idx = tid; idx < BZ * nz; idx += nt) {
-    const int b = idx >> lognz, zi = idx & (nz - 1);
-    if (b >= bv) continue;
-    const int e = ((zi >> 1) * P + b) * 2 + (zi & 1);  // scalar index in a tile
-    T dx = tl[e], dy = tl[2 * TS + e], dz = tl[4 * TS + e], lp = tl[6 * TS + e];
-    const long long gi = (r0 + b) * nz + zi;
-    T phi = yfl[gi], dph = yfl[N + gi], ps = yfl[2 * N + gi];
-    T grad = dx * dx;
-    grad += dy * dy;
-    grad += dz * dz;
-    T rho, p;
-    if (!MIXED) {
-      T t1 = ((T)0.5 - ps) * dph * dph;
-      T t2 = ((T)0.5 + ps) * grad * inv_a2;
-      T V = m2 * phi * phi * (T)0.5;
-      rho = t1 + t2 + V;
-      p = t1 - t2 * third - V;
-    } else {
-      const T phib = (T)ysc[0], pib = (T)ysc[1], psib = (T)ysc[2];
-      T pif = pib + dph;
-      T kin = ((T)0.5 - psib) * ((T)2.0 * pib * dph + dph * dph) - ps * pif * pif;
-      T grd = ((T)0.5 + psib + ps) * grad * inv_a2;
-      T pot = m2 * phib * phi + (T)0.5 * m2 * phi * phi;
-      rho = kin + grd + pot;
-      p = kin - grd * third - pot;
-    }
-    lap[gi] = lp;
-    pout[gi] = p;
-    if (rhoout) rhoout[gi] = rho;
-    srho += rho;
-    sp += p;
-    if (gw) {
-      // in place: the same thread owns this point in every tile
-      tl[e] = dx * dx;
-      tl[2 * TS + e] = dx * dy;
-      tl[4 * TS + e] = dx * dz;
-      tl[6 * TS + e] = dy * dy;
-      tl[8 * TS + e] = dy * dz;
-      tl[10 * TS + e] = dz * dz;
+  const T phib = (T)ysc[0], pib = (T)ysc[1], psib = (T)ysc[2];
+  T srho = 0, sp = 0;  // per-lane partials (2R points), then FP64
+  if (valid) {
+#pragma unroll
+    for (int n = 0; n < R; ++n) {
+      const long long e = row * (2 * H) + 2 * (t + W * n);
+      const C2<T> phi = *reinterpret_cast<const C2<T> *>(yfl + e);
+      const C2<T> dph = *reinterpret_cast<const C2<T> *>(yfl + N + e);
+      const C2<T> ps = *reinterpret_cast<const C2<T> *>(yfl + 2 * N + e);
+      C2<T> rho, p;
+      rho_p<T, MIXED>(d[0][n].x, d[1][n].x, d[2][n].x, phi.x, dph.x, ps.x, inv_a2, m2, third, phib, pib,
+                      psib, rho.x, p.x);
+      rho_p<T, MIXED>(d[0][n].y, d[1][n].y, d[2][n].y, phi.y, dph.y, ps.y, inv_a2, m2, third, phib, pib,
+                      psib, rho.y, p.y);
+      *reinterpret_cast<C2<T> *>(lap + e) = d[3][n];
+      *reinterpret_cast<C2<T> *>(pout + e) = p;
+      if (rhoout) *reinterpret_cast<C2<T> *>(rhoout + e) = rho;
+      srho += rho.x + rho.y;
+      sp += p.x + p.y;
     }
   }
   // block reduction of the two sums (FP64)
   double dr = (double)srho, dp = (double)sp;
+#pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     dr += __shfl_down_sync(0xffffffffu, dr, o);
     dp += __shfl_down_sync(0xffffffffu, dp, o);
   }
-  const int lane = tid & 31, wid = tid >> 5;
   if (lane == 0) {
-    red[0][wid] = dr;
-    red[1][wid] = dp;
+    red[0][warp] = dr;
+    red[1][warp] = dp;
   }
   __syncthreads();
-  if (tid == 0) {
-    double a = 0.0, b = 0.0;
-    for (int w = 0; w < (nt + 31) / 32; ++w) {
-      a += red[0][w];
-      b += red[1][w];
+  if (threadIdx.x == 0) {
+    double sa = 0.0, sb = 0.0;
+#pragma unroll
+    for (int k = 0; k < WPB; ++k) {
+      sa += red[0][k];
+      sb += red[1][k];
     }
-    partials[2 * blockIdx.x] = a;
-    partials[2 * blockIdx.x + 1] = b;
+    partials[2 * blockIdx.x] = sa;
+    partials[2 * blockIdx.x + 1] = sb;
   }
   if (!gw) return;
-  for (int a = 0; a < 6; ++a) smem_fft<T, BZ, kFftK>(tile + a * TS, h, P, tw, -1, tid, nt);
-  for (int a = 0; a < 6; ++a) {
-    C2<T> *dst = (a < 4 ? s6 + a * sstride4 : s6b + (a - 4) * sstride4) + r0 * mz;
-    const C2<T> *s = tile + a * TS;
-    for (int b = 0; b < bv; ++b)
-      for (int k = tid; k < mz; k += nt) dst[(long long)b * mz + k] = zr2c_post<T>(s, k, h, P, b, wz);
+  // the six GW source products d_i phi d_j phi, forward transforms
+  C2<T> *srow = stage + (warp * Gm::G + gi) * Gm::PS;
+#pragma unroll 1
+  for (int pr = 0; pr < 6; ++pr) {
+    const int ia = pr < 3 ? 0 : (pr < 5 ? 1 : 2);
+    const int ib = pr < 3 ? pr : (pr < 5 ? pr - 2 : 2);
+    C2<T> u[R];
+#pragma unroll
+    for (int n = 0; n < R; ++n) {
+      const C2<T> x = ia == 0 ? d[0][n] : (ia == 1 ? d[1][n] : d[2][n]);
+      const C2<T> y = ib == 0 ? d[0][n] : (ib == 1 ? d[1][n] : d[2][n]);
+      u[n] = mk2<T>(x.x * y.x, x.y * y.y);
+    }
+    zfft_dif<-1, T, H>(u, w, twh);
+    C2<T> xH;
+    zr2c_post_lanes<T, H>(u, t, lane & ~(W - 1), twz, xH);
+    C2<T> *dst = (pr < 4 ? s6 + pr * sstride4 : s6b + (pr - 4) * sstride4) + row * (H + 1);
+    zstore_row<T, H>(u, xH, t, srow, dst, valid);
   }
 }
 
 // ---------------------------------------------------------------------------
 // host launchers
-// threads for a tile of B pencils of length L: B*L/(4K) radix-4 butterflies
-// per stage, at most K per thread
-static int threads_for(int L, int B) {
-  int nt = (L * B + 4 * kFftK - 1) / (4 * kFftK);
-  nt = (nt + 31) / 32 * 32;
-  if (nt < 64) nt = 64;
-  return nt;
-}
 
-// rows per CTA of the z passes, and of the fused z pass (6 tiles)
-template <typename T> constexpr int zrows() { return 8; }
-template <typename T> constexpr int zrows_fused() { return sizeof(T) == 4 ? 8 : 4; }
+// rows of a z-pass CTA
+template <typename T, int H> constexpr int zrows() { return zwarps<T>() * ZGeo<H>::G; }
 
 template <typename T>
 static const C2<T> *tab(void *p) {
   return reinterpret_cast<const C2<T> *>(p);
 }
 
+
+// size dispatch: calls f.template run<L>() for the power of two L
+template <typename F>
+static int dispatch_len(int L, F &&f, bool allow512) {
+  switch (L) {
+    case 4: return f.template run<4>();
+    case 8: return f.template run<8>();
+    case 16: return f.template run<16>();
+    case 32: return f.template run<32>();
+    case 64: return f.template run<64>();
+    case 128: return f.template run<128>();
+    case 256: return f.template run<256>();
+    case 512:
+      if (allow512) return f.template run<512>();
+      break;
+    default:
+      break;
+  }
+  return IH_ERR_ARG;
+}
+
+template <typename T> constexpr bool allow512() { return sizeof(T) == 4; }
+
+// threads of a Stockham tile: B*L/(4K) radix-4 butterflies, at most K each
+static int threads_st(int L, int B) {
+  int nt = (L * B + 4 * kFftK - 1) / (4 * kFftK);
+  nt = (nt + 31) / 32 * 32;
+  return nt < 64 ? 64 : nt;
+}
+
+template <typename T>
+struct XYLaunch {
+  Ctx *c;
+  C2<T> *data;
+  long long stride;
+  int count, axis, sign, var;
+  template <int B>
+  int run_st(int L, dim3 grid, long long sj, long long so, const C2<T> *tw) {
+    const size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * (B + 1));
+    cudaFuncSetAttribute(k_fft_xy_st<T, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_fft_xy_st<T, B><<<grid, threads_st(L, B), sm, c->stream>>>(data, stride, L, sj, so, c->g.mz,
+                                                                  sign, tw);
+    return IH_OK;
+  }
+  template <int L, int B>
+  int run_2s(dim3 grid, long long sj, long long so, const C2<T> *tw) {
+    const size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * (B + 1));
+    cudaFuncSetAttribute(k_fft_xy_2s<T, L, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_fft_xy_2s<T, L, B><<<grid, pass_threads<L, B>(), sm, c->stream>>>(data, stride, sj, so,
+                                                                         c->g.mz, sign, tw);
+    return IH_OK;
+  }
+  template <int L>
+  int run() {
+    if constexpr (L == 512 && !allow512<T>()) {
+      return IH_ERR_ARG;
+    } else {
+      constexpr int B = tileB<T>();
+      const Geom &g = c->g;
+      const long long sj = axis == 0 ? (long long)g.ny * g.mz : g.mz;
+      const long long so = axis == 0 ? g.mz : (long long)g.ny * g.mz;
+      const int outer = axis == 0 ? g.ny : g.nx;
+      const C2<T> *tw = tab<T>(axis == 0 ? c->tw_x : c->tw_y);
+      const int bw = var == FV_TWOSTEP_HALF ? B / 2 : B;
+      dim3 grid((g.mz + bw - 1) / bw, outer, count);
+      if (var == FV_TWOSTEP) return run_2s<L, B>(grid, sj, so, tw);
+      if (var == FV_TWOSTEP_HALF) return run_2s<L, B / 2>(grid, sj, so, tw);
+      return run_st<B>(L, grid, sj, so, tw);
+    }
+  }
+};
+
 template <typename T>
 int fft_xy(Ctx *c, C2<T> *data, long long stride, int count, int axis, int sign) {
-  constexpr int B = tileB<T>();
   const Geom &g = c->g;
   const int L = axis == 0 ? g.nx : g.ny;
-  const long long sj = axis == 0 ? (long long)g.ny * g.mz : g.mz;
-  const long long so = axis == 0 ? g.mz : (long long)g.ny * g.mz;
-  const int outer = axis == 0 ? g.ny : g.nx;
-  dim3 grid((g.mz + B - 1) / B, outer, count);
-  const int nt = threads_for(L, B);
-  size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * (B + 1));
-  cudaFuncSetAttribute(k_fft_xy<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   prof_begin(c, KK_FFT_XY);
-  k_fft_xy<T><<<grid, nt, sm, c->stream>>>(data, stride, L, sj, so, g.mz, sign,
-                                             tab<T>(axis == 0 ? c->tw_x : c->tw_y));
+  IH_TRY(dispatch_len(L, XYLaunch<T>{c, data, stride, count, axis, sign, c->xy_var[axis]},
+                      allow512<T>()));
   prof_end(c, KK_FFT_XY, 2.0 * count * g.M * sizeof(C2<T>));
   return check_launch(c, "k_fft_xy");
 }
 
 template <typename T>
+struct ZLaunch {
+  Ctx *c;
+  const void *in;
+  long long istride;
+  void *out;
+  long long ostride;
+  int count;
+  bool forward;
+  template <int H>
+  int run() {
+    if constexpr (H > 256) {
+      return IH_ERR_ARG;
+    } else {
+      constexpr int RB = zrows<T, H>();
+      const Geom &g = c->g;
+      const long long rows = (long long)g.nx * g.ny;
+      dim3 grid((unsigned)((rows + RB - 1) / RB), count, 1);
+      const int nt = 32 * zwarps<T>();
+      if (forward) {
+        k_fft_zr2c<T, H><<<grid, nt, 0, c->stream>>>((const T *)in, istride, (C2<T> *)out, ostride,
+                                                     rows, tab<T>(c->tw_h), tab<T>(c->tw_z));
+      } else {
+        k_fft_zc2r<T, H><<<grid, nt, 0, c->stream>>>((const C2<T> *)in, istride, (T *)out, ostride,
+                                                     rows, tab<T>(c->tw_h), tab<T>(c->tw_z));
+      }
+      return IH_OK;
+    }
+  }
+};
+
+template <typename T>
 int fft_zr2c(Ctx *c, const T *in, long long in_stride, C2<T> *out, long long out_stride,
              int count) {
-  constexpr int BZ = zrows<T>();
   const Geom &g = c->g;
-  const long long rows = (long long)g.nx * g.ny;
-  dim3 grid((unsigned)((rows + BZ - 1) / BZ), 1, count);
-  const int nt = threads_for(g.h, BZ);
-  size_t sm = sizeof(C2<T>) * ((size_t)2 * g.h + 1 + (size_t)g.h * (BZ + 1));
-  cudaFuncSetAttribute(k_fft_zr2c<T, BZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   prof_begin(c, KK_FFT_ZR2C);
-  k_fft_zr2c<T, BZ><<<grid, nt, sm, c->stream>>>(in, in_stride, out, out_stride, rows, g.h,
-                                                   ilog2(g.h), tab<T>(c->tw_h), tab<T>(c->tw_z));
+  IH_TRY(dispatch_len(g.h, ZLaunch<T>{c, in, in_stride, out, out_stride, count, true}, false));
   prof_end(c, KK_FFT_ZR2C, (double)count * (g.N * sizeof(T) + g.M * sizeof(C2<T>)));
   return check_launch(c, "k_fft_zr2c");
 }
@@ -550,16 +961,9 @@ int fft_zr2c(Ctx *c, const T *in, long long in_stride, C2<T> *out, long long out
 template <typename T>
 int fft_zc2r(Ctx *c, const C2<T> *in, long long in_stride, T *out, long long out_stride,
              int count) {
-  constexpr int BZ = zrows<T>();
   const Geom &g = c->g;
-  const long long rows = (long long)g.nx * g.ny;
-  dim3 grid((unsigned)((rows + BZ - 1) / BZ), 1, count);
-  const int nt = threads_for(g.h, BZ);
-  size_t sm = sizeof(C2<T>) * ((size_t)2 * g.h + 1 + (size_t)g.h * (BZ + 1));
-  cudaFuncSetAttribute(k_fft_zc2r<T, BZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   prof_begin(c, KK_FFT_ZC2R);
-  k_fft_zc2r<T, BZ><<<grid, nt, sm, c->stream>>>(in, in_stride, out, out_stride, rows, g.h,
-                                                   ilog2(g.h), tab<T>(c->tw_h), tab<T>(c->tw_z));
+  IH_TRY(dispatch_len(g.h, ZLaunch<T>{c, in, in_stride, out, out_stride, count, false}, false));
   prof_end(c, KK_FFT_ZC2R, (double)count * (g.N * sizeof(T) + g.M * sizeof(C2<T>)));
   return check_launch(c, "k_fft_zc2r");
 }
@@ -582,54 +986,108 @@ int fft_c2r(Ctx *c, C2<T> *in, long long in_stride, T *out, long long out_stride
 }
 
 template <typename T>
+struct D4Launch {
+  Ctx *c;
+  const C2<T> *phihat;
+  C2<T> *out;
+  long long out_stride;
+  int var;
+  template <int L, int B>
+  int run_2s() {
+    const Geom &g = c->g;
+    dim3 grid((g.mz + B - 1) / B, g.ny, 1);
+    const size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * (B + 1));
+    cudaFuncSetAttribute(k_fft_x_deriv4_2s<T, L, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm);
+    k_fft_x_deriv4_2s<T, L, B><<<grid, pass_threads<L, B>(), sm, c->stream>>>(
+        phihat, out, out_stride, g, tab<T>(c->tw_x));
+    return IH_OK;
+  }
+  template <int L>
+  int run() {
+    if constexpr (L == 512 && !allow512<T>()) {
+      return IH_ERR_ARG;
+    } else {
+      constexpr int B = tileB<T>();
+      if (var == FV_TWOSTEP) return run_2s<L, B>();
+      if (var == FV_TWOSTEP_HALF) return run_2s<L, B / 2>();
+      const Geom &g = c->g;
+      dim3 grid((g.mz + B - 1) / B, g.ny, 1);
+      const size_t sm = sizeof(C2<T>) * ((size_t)L + 2 * (size_t)L * (B + 1));
+      cudaFuncSetAttribute(k_fft_x_deriv4_st<T, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sm);
+      k_fft_x_deriv4_st<T, B><<<grid, threads_st(L, B), sm, c->stream>>>(phihat, out, out_stride,
+                                                                          g, tab<T>(c->tw_x));
+      return IH_OK;
+    }
+  }
+};
+
+template <typename T>
 int fft_x_deriv4_inv(Ctx *c, const C2<T> *phihat, C2<T> *out, long long out_stride) {
-  constexpr int B = tileB<T>();
   const Geom &g = c->g;
-  dim3 grid((g.mz + B - 1) / B, g.ny, 1);
-  const int nt = threads_for(g.nx, B);
-  size_t sm = sizeof(C2<T>) * ((size_t)g.nx + 2 * (size_t)g.nx * (B + 1));
-  cudaFuncSetAttribute(k_fft_x_deriv4_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   prof_begin(c, KK_X_DERIV4);
-  k_fft_x_deriv4_inv<T><<<grid, nt, sm, c->stream>>>(phihat, out, out_stride, g, tab<T>(c->tw_x));
+  IH_TRY(dispatch_len(g.nx, D4Launch<T>{c, phihat, out, out_stride, c->d4_var}, allow512<T>()));
   prof_end(c, KK_X_DERIV4, 5.0 * g.M * sizeof(C2<T>));
   return check_launch(c, "k_fft_x_deriv4_inv");
 }
 
 template <typename T>
+struct FusedLaunch {
+  Ctx *c;
+  const C2<T> *d4;
+  const T *yfl;
+  const double *ysc;
+  T *lap, *p, *rho;
+  C2<T> *s6;
+  int gw;
+  double *partials;
+  int *nblk_out;
+  template <int H>
+  int run() {
+    if constexpr (H > 256) {
+      return IH_ERR_ARG;
+    } else {
+      constexpr int RB = zrows<T, H>();
+      const Geom &g = c->g;
+      const long long rows = (long long)g.nx * g.ny;
+      const unsigned nblk = (unsigned)((rows + RB - 1) / RB);
+      if (2LL * nblk > c->partials_cap) {
+        c->err = "grid too large for the RHS partial-sum buffer";
+        return IH_ERR_ARG;
+      }
+      const int nt = 32 * zwarps<T>();
+      const long long M = g.M;
+      C2<T> *s6b = s6 + 5 * M;  // products 4 and 5 go to spec[5], spec[6]
+      if (c->mixed) {
+        if constexpr (sizeof(T) == 4) {
+          k_fft_z_rhs_fused<T, true, H><<<nblk, nt, 0, c->stream>>>(
+              d4, M, yfl, ysc, lap, p, rho, s6, M, s6b, gw, partials, g, tab<T>(c->tw_h),
+              tab<T>(c->tw_z));
+        }
+      } else {
+        if constexpr (sizeof(T) == 8) {
+          k_fft_z_rhs_fused<T, false, H><<<nblk, nt, 0, c->stream>>>(
+              d4, M, yfl, ysc, lap, p, rho, s6, M, s6b, gw, partials, g, tab<T>(c->tw_h),
+              tab<T>(c->tw_z));
+        }
+      }
+      *nblk_out = (int)nblk;
+      return IH_OK;
+    }
+  }
+};
+
+template <typename T>
 int fft_z_rhs_fused(Ctx *c, const C2<T> *d4, const T *yfl, const double *ysc, T *lap, T *p,
                     T *rho, C2<T> *s6, int gw, double *partials, int *nblocks_out) {
-  constexpr int BZ = zrows_fused<T>();
   const Geom &g = c->g;
-  const long long rows = (long long)g.nx * g.ny;
-  const unsigned nblk = (unsigned)((rows + BZ - 1) / BZ);
-  if (2LL * nblk > c->partials_cap) {
-    c->err = "grid too large for the RHS partial-sum buffer";
-    return IH_ERR_ARG;
-  }
-  int nt = threads_for(g.h, BZ);
-  if (nt < 256) nt = 256;
-  size_t sm = sizeof(C2<T>) * ((size_t)2 * g.h + 1 + 6 * (size_t)g.h * (BZ + 1));
-  const long long M = g.M;
-  C2<T> *s6b = s6 + 5 * M;  // products 4 and 5 go to spec[5], spec[6]
-  const int logh = ilog2(g.h);
   prof_begin(c, KK_Z_RHS_FUSED);
-  if (c->mixed) {
-    cudaFuncSetAttribute(k_fft_z_rhs_fused<T, true, BZ>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_fft_z_rhs_fused<T, true, BZ><<<nblk, nt, sm, c->stream>>>(
-        d4, M, yfl, ysc, lap, p, rho, s6, M, s6b, gw, partials, g, logh, tab<T>(c->tw_h),
-        tab<T>(c->tw_z));
-  } else {
-    cudaFuncSetAttribute(k_fft_z_rhs_fused<T, false, BZ>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_fft_z_rhs_fused<T, false, BZ><<<nblk, nt, sm, c->stream>>>(
-        d4, M, yfl, ysc, lap, p, rho, s6, M, s6b, gw, partials, g, logh, tab<T>(c->tw_h),
-        tab<T>(c->tw_z));
-  }
+  IH_TRY(dispatch_len(g.h, FusedLaunch<T>{c, d4, yfl, ysc, lap, p, rho, s6, gw, partials, nblocks_out},
+                      false));
   prof_end(c, KK_Z_RHS_FUSED,
-           (double)(4 + (gw ? 6 : 0)) * M * sizeof(C2<T>) +
+           (double)(4 + (gw ? 6 : 0)) * g.M * sizeof(C2<T>) +
                (double)(3 + 2 + (rho ? 1 : 0)) * g.N * sizeof(T));
-  *nblocks_out = (int)nblk;
   return check_launch(c, "k_fft_z_rhs_fused");
 }
 
@@ -662,6 +1120,80 @@ int fft_tables(Ctx *c) {
     IH_TRY(upload_table<double>(c, &c->tw_z, g.nz));
   }
   return IH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// autotuner: every engine variant of the x/y passes (per axis, on four
+// arrays, the largest batch the RHS issues) and of the fused x pass, timed
+// with CUDA events on the context stream over zeroed scratch spectra; the
+// fastest is kept.  Transform timing does not depend on the data.
+static const char *variant_name(int v) {
+  return v == FV_STOCKHAM ? "stockham" : (v == FV_TWOSTEP ? "two-step" : "two-step-half");
+}
+
+template <typename T>
+static int autotune_t(Ctx *c) {
+  const Geom &g = c->g;
+  const long long M = g.M;
+  C2<T> *sp = reinterpret_cast<C2<T> *>(c->spec[0]);
+  IH_CUDA(c, cudaMemsetAsync(sp, 0, sizeof(C2<T>) * 7 * (size_t)M, c->stream));
+  cudaEvent_t e0, e1;
+  IH_CUDA(c, cudaEventCreate(&e0));
+  IH_CUDA(c, cudaEventCreate(&e1));
+  const int prof = c->prof_on;
+  c->prof_on = 0;
+  const int reps = 3;
+  char line[160];
+  std::string rep;
+  int st = IH_OK;
+  for (int pass = 0; pass < 3 && st == IH_OK; ++pass) {  // x, y, fused x
+    int best = 0;
+    float tbest = 0.f;
+    for (int v = 0; v < FV_COUNT && st == IH_OK; ++v) {
+      if (pass < 2) {
+        c->xy_var[pass] = v;
+      } else {
+        c->d4_var = v;
+      }
+      float ms = 0.f;
+      for (int r = 0; r <= reps && st == IH_OK; ++r) {  // r = 0: warm-up
+        if (r == 1) cudaEventRecord(e0, c->stream);
+        st = pass < 2 ? fft_xy<T>(c, sp, M, 4, pass, -1) : fft_x_deriv4_inv<T>(c, sp + 4 * M, sp, M);
+      }
+      if (st != IH_OK) break;
+      cudaEventRecord(e1, c->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        c->err = "autotune: event timing failed";
+        st = IH_ERR_CUDA;
+        break;
+      }
+      ms /= reps;
+      snprintf(line, sizeof line, "%s %s %.1f us; ", pass == 0 ? "x" : (pass == 1 ? "y" : "deriv4-x"),
+               variant_name(v), 1e3 * ms);
+      rep += line;
+      if (v == 0 || ms < tbest) {
+        best = v;
+        tbest = ms;
+      }
+    }
+    if (pass < 2) {
+      c->xy_var[pass] = best;
+    } else {
+      c->d4_var = best;
+    }
+  }
+  c->prof_on = prof;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != IH_OK) return st;
+  snprintf(line, sizeof line, "chosen: x %s, y %s, deriv4-x %s", variant_name(c->xy_var[0]),
+           variant_name(c->xy_var[1]), variant_name(c->d4_var));
+  c->tune_report = rep + line;
+  return IH_OK;
+}
+
+int fft_autotune(Ctx *c) {
+  return c->mixed ? autotune_t<float>(c) : autotune_t<double>(c);
 }
 
 #define IH_INST(T)                                                                              \

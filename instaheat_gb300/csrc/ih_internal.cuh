@@ -116,12 +116,17 @@ struct Ctx {
   long long partials_cap = 0;
   RhsScalars *rs = nullptr;     // device
   RhsScalars rs_host{};
-  double *diag = nullptr;       // device: 4 spectra * bins + 4 cstr + 24 smry + misc
+  // device, 4 * bins + 128 doubles: 4 spectra, then (offsets after 4 * bins)
+  // 0-27 constraints + summaries, 28-29 means, 40-42 psi means, 48-50 error
+  // sums, 64-67 means of the reference layout, 72-83 error breakdown,
+  // 100-101 rms, 112-113 host-array mean / variance
+  double *diag = nullptr;
   double *hpin = nullptr;       // pinned host staging: small values
   size_t hpin_bytes = 0;
 
   // state and stepper vectors
   Vec y, ynew, ytmp, k[13];     // k[1..12] stage RHS, k[1] = dfield
+  int step_start_valid = 0;     // ynew holds the state at the start of the last step
   double t = 0.0;
   int have_state = 0, dopri_ready = 0;
   ih_dopri_cfg cfg{};
@@ -148,6 +153,20 @@ struct Ctx {
 
   // last output flag results available
   int have_output = 0;
+
+  // FFT engines of the x/y passes (per axis) and of the fused x pass, chosen
+  // by fft_autotune; Stockham with 128-byte tiles until tuned
+  int xy_var[2] = {0, 0};
+  int d4_var = 0;
+  std::string tune_report;
+};
+
+// FFT engine variants (fft_autotune picks one per pass)
+enum FftVariant {
+  FV_STOCKHAM = 0,      // shared-memory Stockham, tile of one 128-byte line of pencils
+  FV_TWOSTEP = 1,       // register two-step, tile of one 128-byte line
+  FV_TWOSTEP_HALF = 2,  // register two-step, tile of half a line
+  FV_COUNT
 };
 
 // ---------------------------------------------------------------------------
@@ -210,6 +229,9 @@ int fft_z_rhs_fused(Ctx *c, const C2<T> *d4, const T *yfl, const double *ysc,
                     int *nblocks_out);
 
 int fft_tables(Ctx *c);
+// time every engine variant of the x/y passes and the fused x pass on the
+// context's scratch spectra and keep the fastest
+int fft_autotune(Ctx *c);
 
 // ---------------------------------------------------------------------------
 // RHS and helpers (ih_rhs.cu)
@@ -217,6 +239,9 @@ int rhs(Ctx *c, double t, Vec &y, Vec &k, int filter, int output,
         const Vec *smry_src);
 int reduce_mean(Ctx *c, const void *arr, long long n, double *dev_out);
 int reduce_mean_f64(Ctx *c, const double *arr, long long n, double *dev_out);
+// variance of n device doubles around `mean` (toolbox.c:744-754) into
+// dev_out[1]; dev_out[0] receives the mean
+int variance_f64(Ctx *c, const double *arr, long long n, double mean, double *dev_out);
 int ic_fluctuations(Ctx *c, uint64_t seed, double phi0, double dphi0,
                     double a0, double amp, double kcut);
 int initial_psi(Ctx *c);
@@ -236,7 +261,7 @@ int step_features(Ctx *c, float *out12);
 int field_rms(Ctx *c, const void *arr, long long n, double *dev_out);
 
 // stepper (ih_stepper.cu)
-int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0);
+int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0, int want_output = 0);
 int dopri_step(Ctx *c, double dt_try, int want_output, ih_step_info *info);
 int rk4_step(Ctx *c, double dt, int want_output);
 void dopri_tableau(double *cc, double *a, double *b, double *bhh, double *er);

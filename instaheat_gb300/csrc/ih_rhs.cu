@@ -725,6 +725,18 @@ static int summary(Ctx *c, const T *a, const double *add_dev_unused, double add,
   return check_launch(c, "k_smry2_finish");
 }
 
+__global__ void k_set_scalar(double *dst, double v) { *dst = v; }
+
+int variance_f64(Ctx *c, const double *arr, long long n, double mean, double *dev_out) {
+  k_set_scalar<<<1, 1, 0, c->stream>>>(dev_out, mean);
+  IH_TRY(check_launch(c, "k_set_scalar"));
+  const int nb = nblk_reduce(n);
+  k_smry2<double><<<nb, 256, 0, c->stream>>>(arr, 0.0, n, dev_out, c->partials);
+  IH_TRY(check_launch(c, "k_smry2"));
+  k_smry2_finish<<<1, 256, 0, c->stream>>>(c->partials, nb, n, dev_out);
+  return check_launch(c, "k_smry2_finish");
+}
+
 // The output flag (toolbox.c:251-270), in two parts around the fused z pass
 // (which reuses spec[0..3], spec[5], spec[6] for the GW products).
 // output_pre: psi power spectrum and the laplacian of psi (toolbox.c:172-184)
@@ -832,7 +844,8 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
   T *yfl = (T *)y.fl, *kfl = (T *)k.fl;
   T *lap = (T *)c->rbuf[0], *p = (T *)c->rbuf[1], *rho = (T *)c->rbuf[2];
   c->calls_rhs += 1;
-  c->have_output = 0;
+  // the diagnostics stay those of the last RHS run with the output flag
+  if (output == 1) c->have_output = 0;
   const int do_filter = (filter == 1) && c->p.enable_filter;
   const unsigned gm = grid_for(M, 256, 4);
   // 1. phihat (and with the filter: dphi, psi, dpsi spectra, mask, write back)

@@ -473,7 +473,7 @@ static int learned_dt(Ctx *c, double dt_did, double rho_mean, double *dt_out) {
   return IH_OK;
 }
 
-int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0) {
+int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0, int want_output) {
   tableau_init();
   for (int j = 1; j <= 12; ++j) IH_TRY(alloc_vec(c, c->k[j]));
   c->cfg = *cfg;
@@ -484,7 +484,7 @@ int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0) {
   c->n_ok = c->n_bad = c->n_stp = c->n_tries = 0;
   c->hist_n = 0;
   // prepare_and_save_timeslice: RHS with the filter on (toolbox.c:96-104)
-  IH_TRY(rhs(c, t0, c->y, c->k[1], 1, 0, nullptr));
+  IH_TRY(rhs(c, t0, c->y, c->k[1], 1, want_output, nullptr));
   c->dopri_ready = 1;
   return IH_OK;
 }
@@ -623,6 +623,7 @@ int dopri_step(Ctx *c, double dt_try, int want_output, ih_step_info *info) {
   c->k[1] = c->k[2];
   c->k[2] = tmp;
   c->t += dt;
+  c->step_start_valid = 1;
   // step history; with a proposer its proposal replaces the controller's
   for (int i = 3; i > 0; --i) {
     c->hist_dt[i] = c->hist_dt[i - 1];
@@ -682,6 +683,7 @@ int rk4_step(Ctx *c, double dt, int want_output) {
   c->y = c->ynew;
   c->ynew = tmp;
   c->t = t + dt;
+  c->step_start_valid = 1;
   return IH_OK;
 }
 

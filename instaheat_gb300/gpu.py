@@ -19,6 +19,7 @@ from . import build as _build
 
 PREC_F64 = 0
 PREC_MIXED = 1
+FFT_STOCKHAM, FFT_TWOSTEP, FFT_TWOSTEP_HALF = 0, 1, 2
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed",
           4: "call out of order", 5: "step size underflow", 6: "non-finite value"}
@@ -143,6 +144,15 @@ def load(build_if_missing: bool = True):
     L.ih_step_features.argtypes = [vp, _fp]
     L.ih_dopri853_set_proposer.argtypes = [vp, vp]
     L.ih_dopri853_error_breakdown.argtypes = [vp, _dp]
+    L.ih_dopri853_init_ex.argtypes = [vp, C.POINTER(DopriCfg), C.c_double, C.c_double, C.c_int]
+    L.ih_mean_host.argtypes = [vp, _dp, C.c_size_t, _dp]
+    L.ih_variance_host.argtypes = [vp, C.c_double, _dp, C.c_size_t, _dp]
+    L.ih_get_step_start_state.argtypes = [vp, _dp]
+    L.ih_autotune.argtypes = [vp]
+    L.ih_autotune_report.restype = C.c_char_p
+    L.ih_autotune_report.argtypes = [vp]
+    L.ih_fft_set_engine.argtypes = [vp, C.c_int, C.c_int]
+    L.ih_fft_get_engine.argtypes = [vp, C.c_int]
     _lib = L
     return L
 
@@ -280,7 +290,7 @@ class Context:
     """One grid on one GPU (wraps ih_context)."""
 
     def __init__(self, n=(32, 32, 32), L=(20.0, 20.0, 20.0), mass=1.0, gw=True,
-                 filter=True, bins=None, precision=PREC_F64, device=0):
+                 filter=True, bins=None, precision=PREC_F64, device=0, autotune=False):
         self.L_ = load()
         nx, ny, nz = n
         self.n = (nx, ny, nz)
@@ -295,6 +305,20 @@ class Context:
             raise IHError(st, "ih_create")
         self.h = h
         self.N, self.M, self.Next, self.Ntot = sizes(nx, ny, nz)
+        if autotune:
+            self.autotune()
+
+    # --- FFT engines ---
+    def autotune(self):
+        """Time the FFT engine variants on the device and keep the fastest."""
+        self._ck(self.L_.ih_autotune(self.h), "ih_autotune")
+        return self.L_.ih_autotune_report(self.h).decode()
+
+    def set_engine(self, pass_, engine):
+        self._ck(self.L_.ih_fft_set_engine(self.h, pass_, engine), "ih_fft_set_engine")
+
+    def engines(self):
+        return tuple(int(self.L_.ih_fft_get_engine(self.h, p)) for p in range(3))
 
     # --- lifecycle ---
     def close(self):
@@ -344,6 +368,25 @@ class Context:
         f = np.zeros(self.Ntot)
         self._ck(self.L_.ih_get_state(self.h, _ptr(f)), "ih_get_state")
         return f
+
+    def step_start_state(self):
+        """The state at the start of the last step, after its filter."""
+        f = np.zeros(self.Ntot)
+        self._ck(self.L_.ih_get_step_start_state(self.h, _ptr(f)), "ih_get_step_start_state")
+        return f
+
+    def mean_host(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        out = np.zeros(1)
+        self._ck(self.L_.ih_mean_host(self.h, _ptr(a), a.size, _ptr(out)), "ih_mean_host")
+        return float(out[0])
+
+    def variance_host(self, mean, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        out = np.zeros(1)
+        self._ck(self.L_.ih_variance_host(self.h, float(mean), _ptr(a), a.size, _ptr(out)),
+                 "ih_variance_host")
+        return float(out[0])
 
     def get_dstate(self, out=None):
         f = np.zeros(self.Ntot) if out is None else out
@@ -424,8 +467,9 @@ class Context:
         self._ck(self.L_.ih_initial_psi(self.h), "ih_initial_psi")
 
     # --- steppers ---
-    def dopri_init(self, cfg: DopriCfg, t0=0.0, dt0=1e-3):
-        self._ck(self.L_.ih_dopri853_init(self.h, C.byref(cfg), t0, dt0), "ih_dopri853_init")
+    def dopri_init(self, cfg: DopriCfg, t0=0.0, dt0=1e-3, output=False):
+        self._ck(self.L_.ih_dopri853_init_ex(self.h, C.byref(cfg), t0, dt0, int(output)),
+                 "ih_dopri853_init_ex")
 
     def dopri_step(self, dt_try, output=False):
         info = StepInfo()

@@ -1,0 +1,84 @@
+"""CPU tests of the C99 drop-in layer: parameters.sh -> header, the host
+build (-std=c99 -Wall -Wextra -Werror), the exported reference symbols, and
+source compatibility with a main.h generated from the reference's own
+template (when the reference tree is present)."""
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from instaheat_gb300 import dropin
+
+HERE = Path(__file__).resolve().parent
+PARAMS = HERE / "dropin"
+REF_SRC = Path(os.environ.get("IH_REFERENCE_SRC", "/root/reference/src"))
+
+# the symbols toolbox.h:15-35, dopri853.h:51 and rk4.h:14 declare
+REFERENCE_SYMBOLS = ["mk_rhs", "prepare_and_save_timeslice", "mk_gradient_squared_and_laplacian",
+                     "mk_rho_and_p", "fft", "ifft", "mean", "variance", "run_dopri853", "run_rk4",
+                     "evo_flags"]
+
+
+def test_read_parameters_like_configure():
+    p = dropin.read_parameters('A="1.0" # comment\n\n# full line\nENABLE_GW="1"\nB=2\n')
+    assert p == {"A": "1.0", "ENABLE_GW": "1", "B": "2"}
+    p = dropin.read_parameters(PARAMS / "parameters_dopri853.sh")
+    assert p["INTEGRATION_METHOD"] == "DOPRI853" and p["GRIDPOINTS_X"] == "16"
+
+
+def test_header_text():
+    p = dropin.read_parameters(PARAMS / "parameters_dopri853.sh")
+    h = dropin.header_text(p)
+    assert "#define GRIDPOINTS_X (16)" in h
+    assert "#define ENABLE_GW\n" in h
+    assert "/* OUTPUT_PSI off */" in h
+    assert '#define DATAPATH ("unused")' in h
+    assert "FFTW_DEFAULT_FLAG" not in h
+    del p["MASS"]
+    with pytest.raises(ValueError, match="MASS"):
+        dropin.header_text(p)
+
+
+def test_render_template_substitution():
+    t = "#define MASS (__MASS__)\n#define __ENABLE_GW__\n#define __OUTPUT_PHI__\n"
+    r = dropin.render_template(t, {"MASS": "4.0", "ENABLE_GW": "1", "OUTPUT_PHI": "0"})
+    assert r == "#define MASS (4.0)\n#define ENABLE_GW\n#define NOT_OUTPUT_PHI\n"
+
+
+@pytest.mark.parametrize("name", ["parameters_dopri853.sh", "parameters_rk4.sh"])
+def test_host_builds_warning_free(tmp_path, name):
+    exe = dropin.build_host(PARAMS / name, tmp_path / "host")
+    assert exe.exists()
+
+
+def test_dropin_object_exports_reference_symbols(tmp_path):
+    dropin.write_header(dropin.read_parameters(PARAMS / "parameters_dopri853.sh"),
+                        tmp_path / "ih_parameters.h")
+    obj = tmp_path / "ih_dropin.o"
+    cc = shutil.which("gcc") or shutil.which("cc")
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-c", "-I", str(tmp_path),
+                    "-I", str(dropin.HERE / "host"), "-I", str(dropin.ROOT / "include"),
+                    str(dropin.HERE / "ih_dropin.c"), "-o", str(obj)], check=True)
+    nm = subprocess.run(["nm", "-g", "--defined-only", str(obj)], capture_output=True, text=True,
+                        check=True).stdout.split()
+    for s in REFERENCE_SYMBOLS:
+        assert s in nm, s
+
+
+@pytest.mark.skipif(not (REF_SRC / "main_template.h").exists(), reason="reference tree absent")
+def test_dropin_compiles_against_reference_generated_headers(tmp_path):
+    """ih_dropin.c against the main.h the reference's configure would make from
+    its own parameters.sh (with FFTW/HDF5 type stubs): syntax-only."""
+    params = dropin.read_parameters(REF_SRC / "parameters.sh")
+    # the reference's default file is 1D and RK4-free; the drop-in needs the
+    # DOPRI853 keys, which it has
+    (tmp_path / "main.h").write_text(
+        dropin.render_template((REF_SRC / "main_template.h").read_text(), params))
+    shutil.copy(REF_SRC / "io.h", tmp_path / "io.h")
+    cc = shutil.which("gcc") or shutil.which("cc")
+    r = subprocess.run([cc, "-std=gnu99", "-fsyntax-only", "-I", str(tmp_path),
+                        "-I", str(PARAMS / "stubs"), "-I", str(dropin.ROOT / "include"),
+                        str(dropin.HERE / "ih_dropin.c")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

@@ -218,3 +218,94 @@ def test_mean_dev_matches_numpy(gpu_mod):
     assert st == 0
     ref = x.double().cpu().numpy().mean()
     assert abs(out.item() - ref) <= 1e-13 * abs(ref)
+
+
+ENGINES = [0, 1, 2]  # Stockham, two-step (128-byte tiles), two-step (64-byte tiles)
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("n", [(16, 16, 16), (64, 32, 16), (128, 64, 32), (256, 16, 8)])
+def test_fft_engines_f64(gpu_mod, oracle_mod, n, engine):
+    """Every x/y engine, every pencil length 8..256: FFTs within 1e-13."""
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
+    for p in range(3):
+        ctx.set_engine(p, engine)
+    assert ctx.engines() == (engine,) * 3
+    o = oracle_mod.Oracle(n=n)
+    x = np.random.default_rng(1).standard_normal(n)
+    R = o.fft(x)
+    assert np.abs(ctx.fft(x) - R).max() <= 1e-13 * np.abs(R).max()
+    yr = o.ifft(R)
+    assert np.abs(ctx.ifft(R) - yr).max() <= 1e-13 * np.abs(yr).max()
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("n", [(32, 32, 32), (512, 16, 8)])
+def test_fft_engines_fp32(gpu_mod, oracle_mod, n, engine):
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
+    for p in range(3):
+        ctx.set_engine(p, engine)
+    o = oracle_mod.Oracle(n=n)
+    x = np.random.default_rng(2).standard_normal(n)
+    R = o.fft(x)
+    assert np.abs(ctx.fft(x) - R).max() <= 3e-6 * np.abs(R).max()
+    yr = o.ifft(R)
+    assert np.abs(ctx.ifft(R) - yr).max() <= 3e-6 * np.abs(yr).max()
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_rhs_engines_f64_parity(gpu_mod, oracle_mod, engine):
+    """The fused inverse x pass of each engine: FP64 RHS within 1e-11."""
+    n = (64, 32, 32)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
+    for p in range(3):
+        ctx.set_engine(p, engine)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=9)
+    r_ref, _ = o.rhs(f, filter=1)
+    r_gpu, _ = ctx.mk_rhs(f, filter=1)
+    errs = seg_rel_err(r_gpu, r_ref, o.N, o.Next)
+    assert max(errs.values()) < 1e-11, errs
+
+
+def test_autotune_picks_an_engine_and_keeps_parity(gpu_mod, oracle_mod):
+    n = (64, 64, 64)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
+    rep = ctx.autotune()
+    assert "chosen:" in rep
+    assert all(e in ENGINES for e in ctx.engines())
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=4)
+    r_ref, _ = o.rhs(f, filter=0)
+    r_gpu, _ = ctx.mk_rhs(f, filter=0)
+    assert max(seg_rel_err(r_gpu, r_ref, o.N, o.Next).values()) < 1e-11
+
+
+def test_mean_variance_host(gpu_mod):
+    """mean / variance (toolbox.c:726-754) of host arrays, computed on the GPU."""
+    ctx = gpu_mod.Context(n=(16, 16, 16), precision=gpu_mod.PREC_F64)
+    a = np.random.default_rng(3).standard_normal(4096) * 3.0 + 1.5
+    m = ctx.mean_host(a)
+    assert abs(m - a.sum() / a.size) <= 1e-14 * abs(m)
+    mu = 1.25  # the caller's mean, not necessarily the exact one
+    v = ctx.variance_host(mu, a)
+    d = a - mu
+    ref = (np.sum(d * d) - np.sum(d) ** 2 / a.size) / (a.size - 1)
+    assert abs(v - ref) <= 1e-13 * ref
+    with pytest.raises(gpu_mod.IHError):
+        ctx.mean_host(np.zeros(ctx.Ntot + 1))
+
+
+def test_step_start_state_is_the_filtered_start(gpu_mod, oracle_mod):
+    """After an RK4 step the library still holds the filtered start state."""
+    n = (16, 16, 16)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=2)
+    ctx.set_state(f)
+    with pytest.raises(gpu_mod.IHError):
+        ctx.step_start_state()
+    ctx.rk4_step(1e-3)
+    s0 = ctx.step_start_state()
+    _, f_filt = o.rhs(f, filter=1)
+    assert np.abs(s0 - f_filt).max() <= 1e-13 * np.abs(f_filt[: 4 * o.N]).max()
