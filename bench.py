@@ -142,7 +142,7 @@ class Clocks:
                 "samples": len(sm)}
 
 
-ENGINE_NAMES = {0: "stockham", 1: "two-step", 2: "two-step-half"}
+ENGINE_NAMES = {0: "stockham", 1: "two-step", 2: "two-step-half", 3: "pipelined"}
 
 
 def make_context(gpu, precision, device):
@@ -198,7 +198,8 @@ def bench_form(gpu, precision, device, seed, steps, warmup, profile=False, clock
     res = {"ms": ms, "mt": mt, "dt_next": dt, "launches": launches, "kernels": kern, "clocks": clk,
            "t": ctx.t, "device_bytes": ctx.device_bytes,
            "fft_engines": dict(zip(("x", "y", "deriv4_x"),
-                                   (ENGINE_NAMES[e] for e in ctx.engines())))}
+                                   (ENGINE_NAMES[e] for e in ctx.engines()))),
+           "fft_autotune": ctx.autotune_report}
     return ctx, res
 
 
@@ -345,7 +346,8 @@ def main():
                        "l2": "inputs larger than L2 (state 1.1 GB)",
                        "dt_next": mixed["dt_next"], "t_reached": mixed["t"],
                        "device_GB": mixed["device_bytes"] / 1e9,
-                       "fft_engines": mixed["fft_engines"]},
+                       "fft_engines": mixed["fft_engines"],
+                       "fft_autotune": mixed["fft_autotune"]},
             "gpu_launches": mixed["launches"],
             "e2e": {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")}
                    | {"value": e2e_val},

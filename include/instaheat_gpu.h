@@ -181,8 +181,10 @@ int ih_autotune(ih_context *c);
 const char *ih_autotune_report(const ih_context *c);
 /* Pin or read the engine of one pass: pass 0 = x, 1 = y, 2 = the fused
  * inverse x pass; engine IH_FFT_STOCKHAM, IH_FFT_TWOSTEP (register two-step,
- * 128-byte tiles) or IH_FFT_TWOSTEP_HALF (64-byte tiles). */
-enum { IH_FFT_STOCKHAM = 0, IH_FFT_TWOSTEP = 1, IH_FFT_TWOSTEP_HALF = 2 };
+ * 128-byte tiles), IH_FFT_TWOSTEP_HALF (64-byte tiles) or IH_FFT_PIPELINED
+ * (register two-step in persistent CTAs that copy the next tile in with
+ * cp.async while transforming the current one). */
+enum { IH_FFT_STOCKHAM = 0, IH_FFT_TWOSTEP = 1, IH_FFT_TWOSTEP_HALF = 2, IH_FFT_PIPELINED = 3 };
 int ih_fft_set_engine(ih_context *c, int pass, int engine);
 int ih_fft_get_engine(const ih_context *c, int pass);
 

@@ -157,6 +157,7 @@ static int create(const ih_params *p, Ctx *c) {
   c->tsize = c->mixed ? 4 : 8;
   c->noise_eta = c->mixed ? kDefaultNoiseEta : 0.0;
   IH_CUDA(c, cudaSetDevice(p->device));
+  IH_CUDA(c, cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, p->device));
   IH_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   const Geom &g = c->g;
   const size_t cs = 2 * c->tsize;  // complex element

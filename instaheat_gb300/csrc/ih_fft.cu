@@ -30,6 +30,8 @@
 //                       sums, and six forward z transforms of the GW source
 //                       products, all on one tile of rows.
 #include <math.h>
+#include <mutex>
+#include <unordered_map>
 #include "ih_internal.cuh"
 
 namespace ih {
@@ -90,9 +92,21 @@ __host__ __device__ constexpr int round_warp(int n) { return n < 32 ? 32 : (n + 
 template <int L, int B> __host__ __device__ constexpr int pass_threads() {
   return round_warp(max_r<L>() * B);
 }
+// exp(-2 pi i m/16) for a compile-time m: the cosines and sines of multiples
+// of pi/8 (cos pi/8, sin pi/8, sqrt(1/2)), correctly rounded in double
+template <typename T>
+__device__ __forceinline__ C2<T> w16(int m) {
+  constexpr double c = 0.92387953251128675613, s = 0.38268343236508977173,
+                   h = 0.70710678118654752440;
+  constexpr double re[16] = {1, c, h, s, 0, -s, -h, -c, -1, -c, -h, -s, 0, s, h, c};
+  constexpr double im[16] = {0, -s, -h, -c, -1, -c, -h, -s, 0, s, h, c, 1, c, h, s};
+  return mk2<T>((T)re[m & 15], (T)im[m & 15]);
+}
+
 // In-register DFT of R points: v[k] <- sum_n v[n] exp(sign 2 pi i nk/R).
-// tw[m * ts] = exp(-2 pi i m/R).  Radix-2 decimation in frequency; the
-// bit-reversed result order is undone by a compile-time register permutation.
+// Radix-2 decimation in frequency; the bit-reversed result order is undone by
+// a compile-time register permutation.  Twiddles are compile-time constants
+// for R <= 16, else tw[m * ts] = exp(-2 pi i m/R).
 template <typename T, int R>
 __device__ __forceinline__ void reg_dft(C2<T> (&v)[R], const C2<T> *tw, int ts, int sign) {
   constexpr int LOGR = clog2(R);
@@ -111,7 +125,7 @@ __device__ __forceinline__ void reg_dft(C2<T> (&v)[R], const C2<T> *tw, int ts, 
         } else if (4 * j == len) {  // exp(sign i pi/2) = sign * i
           v[st + j + half] = mk2<T>(-(T)sign * d.y, (T)sign * d.x);
         } else {
-          C2<T> w = tw[j * (R / len) * ts];
+          C2<T> w = (R <= 16) ? w16<T>(j * (16 / len)) : tw[j * (R / len) * ts];
           if (sign > 0) w.y = -w.y;
           v[st + j + half] = cmul(d, w);
         }
@@ -314,6 +328,118 @@ __global__ void __launch_bounds__(pass_threads<L, B>()) k_fft_xy_2s(C2<T> *data,
 }
 
 // ---------------------------------------------------------------------------
+// Pipelined two-step engine: persistent CTAs walk the tiles of the pass; the
+// next tile is copied global -> shared with cp.async while the current one is
+// transformed, so every CTA keeps a whole tile of loads in flight (the plain
+// engines idle their loads during the arithmetic).  The tile buffer is
+// [L][B] without padding -- a row is one 128-byte line (or half), so the
+// line-wise accesses of both steps are free of bank conflicts -- and after
+// step 1 has read it into registers it is reused for the exchange.
+template <typename T>
+__device__ __forceinline__ void cp_async_c(C2<T> *s, const C2<T> *g, bool valid) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
+  if constexpr (sizeof(T) == 4) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(g),
+                 "r"(valid ? 8 : 0)
+                 : "memory");
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(g),
+                 "r"(valid ? 16 : 0)
+                 : "memory");
+  }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// tile t of a pass -> its first element and the valid pencils of the tile
+struct XYTiles {
+  long long astride, so;
+  int mz, ntz, outer;
+  template <typename V>
+  __device__ __forceinline__ V *base(V *data, long long t, int B, int &bv) const {
+    const int zt = (int)(t % ntz);
+    const long long r = t / ntz;
+    const int o = (int)(r % outer);
+    const long long a = r / outer;
+    const int z0 = zt * B;
+    bv = min(B, mz - z0);
+    return data + a * astride + (long long)o * so + z0;
+  }
+};
+
+// copy tile t into buf (masked pencils zero-filled, nothing read for them)
+template <typename T, int L, int B>
+__device__ __forceinline__ void tile_prefetch(const C2<T> *data, const XYTiles &tl, long long t,
+                                              long long sj, C2<T> *buf) {
+  constexpr int LB = clog2(B);
+  int bv;
+  const C2<T> *base = tl.base(data, t, B, bv);
+  for (int idx = threadIdx.x; idx < L * B; idx += blockDim.x) {
+    const int b = idx & (B - 1), j = idx >> LB;
+    const bool ok = b < bv;
+    cp_async_c<T>(buf + idx, ok ? base + (long long)j * sj + b : base, ok);
+  }
+  cp_async_commit();
+}
+
+template <typename T, int L, int B>
+__global__ void __launch_bounds__(pass_threads<L, B>(), 2) k_fft_xy_pipe(C2<T> *data, long long sj, XYTiles tl, long long total,
+                                             int sign, const C2<T> *twg) {
+  constexpr int R1 = Fac<L>::R1, R2 = Fac<L>::R2;
+  constexpr int LB = clog2(B);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<T> *tw = reinterpret_cast<C2<T> *>(smraw);
+  C2<T> *buf0 = tw + L;  // two tiles [L][B]
+  const int tid = threadIdx.x;
+  load_table(tw, twg, L, tid, blockDim.x);
+  long long t = blockIdx.x;
+  if (t < total) tile_prefetch<T, L, B>(data, tl, t, sj, buf0);
+  const int b = tid & (B - 1), n1 = tid >> LB;
+  for (int cur = 0; t < total; t += gridDim.x, cur ^= 1) {
+    C2<T> *bc = buf0 + cur * L * B;
+    const long long tn = t + gridDim.x;
+    if (tn < total) {
+      tile_prefetch<T, L, B>(data, tl, tn, sj, buf0 + (cur ^ 1) * L * B);
+    } else {
+      cp_async_commit();  // an empty group keeps the wait count uniform
+    }
+    cp_async_wait<1>();
+    __syncthreads();
+    C2<T> v[R2];
+    if (tid < R1 * B) {
+#pragma unroll
+      for (int n2 = 0; n2 < R2; ++n2) v[n2] = bc[(n1 + R1 * n2) * B + b];
+      reg_dft<T, R2>(v, tw, L / R2, sign);
+    }
+    __syncthreads();
+    if (tid < R1 * B) {
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2)
+        bc[(n1 * R2 + k2) * B + b] = (k2 == 0) ? v[k2] : cmul(v[k2], twid(tw, (n1 * k2) & (L - 1), sign));
+    }
+    __syncthreads();
+    if (tid < R2 * B) {
+      const int k2 = tid >> LB;
+      C2<T> u[R1];
+#pragma unroll
+      for (int m1 = 0; m1 < R1; ++m1) u[m1] = bc[(m1 * R2 + k2) * B + b];
+      reg_dft<T, R1>(u, tw, L / R1, sign);
+      int bv;
+      C2<T> *base = tl.base(data, t, B, bv);
+      if (b < bv) {
+#pragma unroll
+        for (int k1 = 0; k1 < R1; ++k1) base[(long long)(k2 + R2 * k1) * sj + b] = u[k1];
+      }
+    }
+    __syncthreads();  // bc is the prefetch target of the next iteration
+  }
+  cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
 // z passes.  A row of H = nz/2 complex values (the real row packed as
 // z_j = x_2j + i x_2j+1) belongs to a group of W = min(32, H) lanes of one
 // warp; each lane holds R = H/W values in one of two index maps:
@@ -332,10 +458,12 @@ template <int H> struct ZGeo {
   static constexpr int LW = clog2(W);
   static constexpr int LR = clog2(R);
   static constexpr int G = 32 / W;  // rows per warp
-  // staging row: H+1 values, one pad slot after every R (breaks the stride-R
-  // bank pattern of the scrambled writes)
-  static constexpr int PS = R > 1 ? H + H / R + 1 : H + 1;
-  __device__ static __forceinline__ int pad(int k) { return R > 1 ? k + (k >> LR) : k; }
+  // staging row of H+1 values, swizzled within blocks of 16: element k sits
+  // at k ^ ((k >> 4) & 15).  A half-warp's scrambled writes (k = k1 + R b,
+  // b = brev(t)) then hit 16 distinct 8-byte bank pairs, as do its natural-
+  // order reads (k = t + W n).
+  static constexpr int PS = H + 16;
+  __device__ static __forceinline__ int pad(int k) { return k ^ ((k >> 4) & 15); }
 };
 
 __device__ __forceinline__ int lane_brev(int t, int lw) {
@@ -400,35 +528,26 @@ __device__ __forceinline__ void zfft_dif(C2<T> (&v)[ZGeo<H>::R], const ZTw<T, H>
   }
 }
 
-// scrambled -> natural, sign S
-template <int S, typename T, int H>
-__device__ __forceinline__ void zfft_dit(C2<T> (&v)[ZGeo<H>::R], const ZTw<T, H> &w,
-                                         const C2<T> *__restrict__ twh) {
-  using Gm = ZGeo<H>;
-#pragma unroll
-  for (int q = 0; q < Gm::LW; ++q) {
-#pragma unroll
-    for (int r = 0; r < Gm::R; ++r) {
-      if (q > 0) v[r] = cmul(v[r], cj<S>(w.st[q]));  // upper lane: twiddle first
-      const C2<T> p = shfl_xor_c(v[r], 1 << q);
-      // lower lane: v + p; upper lane: p - v
-      v[r] = mk2<T>(fma(w.sg[q], v[r].x, p.x), fma(w.sg[q], v[r].y, p.y));
-    }
-  }
-#pragma unroll
-  for (int k1 = 1; k1 < Gm::R; ++k1) v[k1] = cmul(v[k1], cj<S>(w.ta[k1]));
-  reg_dft<T, Gm::R>(v, twh, H / Gm::R, S);
-}
-
 // r2c post-processing of a forward-transformed row held scrambled:
 // X_k = E_k + exp(-2 pi i k/nz) O_k with E_k = (Z_k + conj Z_(H-k))/2 and
 // O_k = (Z_k - conj Z_(H-k))/(2i).  v[k1] = Z_k on entry, X_k on return
 // (k = k1 + R brev(t)); xH = X_H, valid on the lane with t == 0.  The partner
 // Z_(H-k) of register k1 > 0 sits in register R-k1 of lane t^(W-1); that of
 // register 0 in register 0 of lane brev((W - brev(t)) mod W).
+// exp(-2 pi i k/nz) at the scrambled positions k = k1 + R brev(t) of lane t,
+// loaded once per warp for the forward post-processing
+template <typename T, int H>
+__device__ __forceinline__ void zr2c_twiddles(const C2<T> *__restrict__ twz, int t,
+                                              C2<T> (&wzl)[ZGeo<H>::R]) {
+  using Gm = ZGeo<H>;
+  const int b = lane_brev(t, Gm::LW);
+#pragma unroll
+  for (int k1 = 0; k1 < Gm::R; ++k1) wzl[k1] = twz[k1 + Gm::R * b];
+}
+
 template <typename T, int H>
 __device__ __forceinline__ void zr2c_post_lanes(C2<T> (&v)[ZGeo<H>::R], int t, int gbase,
-                                                const C2<T> *__restrict__ twz, C2<T> &xH) {
+                                                const C2<T> (&wzl)[ZGeo<H>::R], C2<T> &xH) {
   using Gm = ZGeo<H>;
   const int b = lane_brev(t, Gm::LW);
   C2<T> pz[Gm::R];
@@ -442,22 +561,63 @@ __device__ __forceinline__ void zr2c_post_lanes(C2<T> (&v)[ZGeo<H>::R], int t, i
     const C2<T> e = mk2<T>((T)0.5 * (z.x + zc.x), (T)0.5 * (z.y + zc.y));
     const C2<T> o = mk2<T>((T)0.5 * (z.y - zc.y), -(T)0.5 * (z.x - zc.x));
     if (k1 == 0) xH = csub(e, o);  // exp(-i pi) = -1
-    v[k1] = cadd(e, cmul(o, twz[k1 + Gm::R * b]));
+    v[k1] = cadd(e, cmul(o, wzl[k1]));
   }
 }
 
-// c2r pre-processing of half-spectrum element k into the packed row:
-// Z_k = E_k + i O_k, E_k = X_k + conj X_(H-k),
-// O_k = (X_k - conj X_(H-k)) exp(+2 pi i k/nz)
-template <typename T>
-__device__ __forceinline__ C2<T> zc2r_pre(const C2<T> *row, int k, int h, const C2<T> *wz) {
-  C2<T> x = row[k], xc = row[h - k];
-  xc.y = -xc.y;
-  C2<T> e = cadd(x, xc), d = csub(x, xc);
-  C2<T> w = wz[k];
-  w.y = -w.y;  // exp(+2 pi i k / nz)
-  C2<T> o = cmul(d, w);
-  return mk2<T>(e.x - o.y, e.y + o.x);  // E + i O
+// c2r input of one half-spectrum row in natural order: lane t, register n
+// receives the packed Z_k = E_k + i O_k, E_k = X_k + conj X_(H-k),
+// O_k = (X_k - conj X_(H-k)) exp(+2 pi i k/nz) (k = t + W n), from
+// line-wise loads of X_k.
+// The partner X_(H-k) is register R-1-n of lane W-t for t > 0 (one indexed
+// shuffle), and lane 0's own X_0 .. X_H for t = 0.
+// exp(+2 pi i k/nz) at the natural positions k = t + W n of lane t
+template <typename T, int H>
+__device__ __forceinline__ void zc2r_twiddles(const C2<T> *__restrict__ twz, int t,
+                                              C2<T> (&wnat)[ZGeo<H>::R]) {
+  using Gm = ZGeo<H>;
+#pragma unroll
+  for (int n = 0; n < Gm::R; ++n) {
+    wnat[n] = twz[t + Gm::W * n];
+    wnat[n].y = -wnat[n].y;
+  }
+}
+
+template <typename T, int H>
+__device__ __forceinline__ void zc2r_load(const C2<T> *row, int t, int gbase, bool valid,
+                                          const C2<T> (&wnat)[ZGeo<H>::R],
+                                          C2<T> (&z)[ZGeo<H>::R]) {
+  using Gm = ZGeo<H>;
+  constexpr int R = Gm::R, W = Gm::W;
+  C2<T> x[R];
+#pragma unroll
+  for (int n = 0; n < R; ++n) x[n] = valid ? row[t + W * n] : mk2<T>(0, 0);
+  const C2<T> xH = (valid && t == 0) ? row[H] : mk2<T>(0, 0);
+  const int src = gbase + ((W - t) & (W - 1));
+#pragma unroll
+  for (int n = 0; n < R; ++n) {
+    C2<T> pc = shfl_idx_c(x[R - 1 - n], src);
+    if (t == 0) pc = (n == 0) ? xH : x[(R - n) % R];
+    pc.y = -pc.y;  // conj X_(H-k)
+    const C2<T> e = cadd(x[n], pc), d = csub(x[n], pc);
+    const C2<T> o = cmul(d, wnat[n]);
+    z[n] = mk2<T>(e.x - o.y, e.y + o.x);  // E + i O
+  }
+}
+
+// a row held scrambled (register k1 of lane t = element k1 + R brev(t))
+// rewritten in natural order (register n of lane t = element t + W n)
+// through the warp's staging row
+template <typename T, int H>
+__device__ __forceinline__ void zunscramble(C2<T> (&v)[ZGeo<H>::R], int t, C2<T> *srow) {
+  using Gm = ZGeo<H>;
+  const int b = lane_brev(t, Gm::LW);
+#pragma unroll
+  for (int k1 = 0; k1 < Gm::R; ++k1) srow[Gm::pad(k1 + Gm::R * b)] = v[k1];
+  __syncwarp();
+#pragma unroll
+  for (int n = 0; n < Gm::R; ++n) v[n] = srow[Gm::pad(t + Gm::W * n)];
+  __syncwarp();
 }
 
 // store a scrambled r2c row (H+1 values) as whole lines through the warp's
@@ -483,6 +643,8 @@ __device__ __forceinline__ void zstore_row(const C2<T> (&v)[ZGeo<H>::R], C2<T> x
 template <typename T> __host__ __device__ constexpr int zwarps() { return sizeof(T) == 4 ? 8 : 4; }
 
 // forward real-to-complex pass along z: rows of nz = 2H reals -> H+1 complex
+// The z-pass CTAs walk the row groups (WPB warps x G rows) with a grid
+// stride, so the per-lane twiddles are loaded once per warp.
 template <typename T, int H>
 __global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_zr2c(const T *in, long long istride, C2<T> *out, long long ostride,
                            long long rows, const C2<T> *__restrict__ twh, const C2<T> *__restrict__ twz) {
@@ -491,19 +653,24 @@ __global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_zr2c(const T *in, long
   __shared__ C2<T> stage[WPB * Gm::G * Gm::PS];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int t = lane & (Gm::W - 1), gi = lane >> Gm::LW;
-  const long long row = ((long long)blockIdx.x * WPB + warp) * Gm::G + gi;
-  const bool valid = row < rows;
   ZTw<T, H> w;
   w.load(twh, t);
-  const C2<T> *src = reinterpret_cast<const C2<T> *>(in + blockIdx.y * istride) + row * H;
-  C2<T> v[Gm::R];
+  C2<T> wzl[Gm::R];
+  zr2c_twiddles<T, H>(twz, t, wzl);
+  C2<T> *srow = stage + (warp * Gm::G + gi) * Gm::PS;
+  const long long ngroups = (rows + WPB * Gm::G - 1) / (WPB * Gm::G);
+  for (long long rg = blockIdx.x; rg < ngroups; rg += gridDim.x) {
+    const long long row = (rg * WPB + warp) * Gm::G + gi;
+    const bool valid = row < rows;
+    const C2<T> *src = reinterpret_cast<const C2<T> *>(in + blockIdx.y * istride) + row * H;
+    C2<T> v[Gm::R];
 #pragma unroll
-  for (int n = 0; n < Gm::R; ++n) v[n] = valid ? src[t + Gm::W * n] : mk2<T>(0, 0);
-  zfft_dif<-1, T, H>(v, w, twh);
-  C2<T> xH;
-  zr2c_post_lanes<T, H>(v, t, lane & ~(Gm::W - 1), twz, xH);
-  zstore_row<T, H>(v, xH, t, stage + (warp * Gm::G + gi) * Gm::PS,
-                   out + blockIdx.y * ostride + row * (H + 1), valid);
+    for (int n = 0; n < Gm::R; ++n) v[n] = valid ? src[t + Gm::W * n] : mk2<T>(0, 0);
+    zfft_dif<-1, T, H>(v, w, twh);
+    C2<T> xH;
+    zr2c_post_lanes<T, H>(v, t, lane & ~(Gm::W - 1), wzl, xH);
+    zstore_row<T, H>(v, xH, t, srow, out + blockIdx.y * ostride + row * (H + 1), valid);
+  }
 }
 
 // inverse complex-to-real pass along z
@@ -512,23 +679,28 @@ __global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_zc2r(const C2<T> *in, 
                            long long rows, const C2<T> *__restrict__ twh, const C2<T> *__restrict__ twz) {
   using Gm = ZGeo<H>;
   constexpr int WPB = zwarps<T>();
+  __shared__ C2<T> stage[WPB * Gm::G * Gm::PS];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int t = lane & (Gm::W - 1), gi = lane >> Gm::LW;
-  const long long row = ((long long)blockIdx.x * WPB + warp) * Gm::G + gi;
-  const bool valid = row < rows;
   ZTw<T, H> w;
   w.load(twh, t);
-  const C2<T> *src = in + blockIdx.y * istride + row * (H + 1);
-  const int b = lane_brev(t, Gm::LW);
-  C2<T> v[Gm::R];
+  C2<T> wnat[Gm::R];
+  zc2r_twiddles<T, H>(twz, t, wnat);
+  C2<T> *srow = stage + (warp * Gm::G + gi) * Gm::PS;
+  const long long ngroups = (rows + WPB * Gm::G - 1) / (WPB * Gm::G);
+  for (long long rg = blockIdx.x; rg < ngroups; rg += gridDim.x) {
+    const long long row = (rg * WPB + warp) * Gm::G + gi;
+    const bool valid = row < rows;
+    C2<T> v[Gm::R];
+    zc2r_load<T, H>(in + blockIdx.y * istride + row * (H + 1), t, lane & ~(Gm::W - 1), valid, wnat,
+                    v);
+    zfft_dif<+1, T, H>(v, w, twh);
+    zunscramble<T, H>(v, t, srow);
+    C2<T> *dst = reinterpret_cast<C2<T> *>(out + blockIdx.y * ostride) + row * H;
+    if (valid) {
 #pragma unroll
-  for (int k1 = 0; k1 < Gm::R; ++k1)
-    v[k1] = valid ? zc2r_pre<T>(src, k1 + Gm::R * b, H, twz) : mk2<T>(0, 0);
-  zfft_dit<+1, T, H>(v, w, twh);
-  C2<T> *dst = reinterpret_cast<C2<T> *>(out + blockIdx.y * ostride) + row * H;
-  if (valid) {
-#pragma unroll
-    for (int n = 0; n < Gm::R; ++n) dst[t + Gm::W * n] = v[n];
+      for (int n = 0; n < Gm::R; ++n) dst[t + Gm::W * n] = v[n];
+    }
   }
 }
 
@@ -702,6 +874,101 @@ __global__ void __launch_bounds__(pass_threads<L, B>(), (d4_min_blocks<T, L, B>(
   }
 }
 
+// Pipelined fused x pass: persistent CTAs, the next phihat tile copied in
+// with cp.async while the four variants of the current one are transformed;
+// the step-1 threads keep their phihat values in registers, so the tile
+// buffer doubles as the exchange buffer.
+template <typename T, int L, int B>
+__global__ void __launch_bounds__(pass_threads<L, B>(), 2) k_fft_x_deriv4_pipe(const C2<T> *phihat, C2<T> *out, long long ostride,
+                                                   XYTiles tl, long long total, Geom g,
+                                                   const C2<T> *twg) {
+  constexpr int R1 = Fac<L>::R1, R2 = Fac<L>::R2;
+  constexpr int LB = clog2(B);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<T> *tw = reinterpret_cast<C2<T> *>(smraw);
+  C2<T> *buf0 = tw + L;  // two tiles [L][B]
+  const int tid = threadIdx.x;
+  load_table(tw, twg, L, tid, blockDim.x);
+  const long long sj = (long long)g.ny * g.mz;
+  const int ny = g.ny, nz = g.nz, nx = g.nx;
+  const T invN = (T)(1.0 / (double)g.N);
+  long long t = blockIdx.x;
+  if (t < total) tile_prefetch<T, L, B>(phihat, tl, t, sj, buf0);
+  const int b = tid & (B - 1), n1 = tid >> LB;
+  const bool s1 = tid < R1 * B;
+  for (int cur = 0; t < total; t += gridDim.x, cur ^= 1) {
+    C2<T> *bc = buf0 + cur * L * B;
+    const long long tn = t + gridDim.x;
+    if (tn < total) {
+      tile_prefetch<T, L, B>(phihat, tl, tn, sj, buf0 + (cur ^ 1) * L * B);
+    } else {
+      cp_async_commit();
+    }
+    cp_async_wait<1>();
+    __syncthreads();
+    // tile coordinates: y index and first z column
+    const int zt = (int)(t % tl.ntz);
+    const int yj = (int)((t / tl.ntz) % tl.outer);
+    const int z0 = zt * B;
+    const int bv = min(B, g.mz - z0);
+    const long long off = (long long)yj * g.mz + z0;
+    const T fy = (2 * yj == ny) ? (T)0 : kfac<T>(g.kyu, (yj > ny / 2) ? (yj - ny) : yj);
+    const int ja = (yj > ny / 2) ? (ny - yj) : yj;
+    const int kz = z0 + b;
+    const T fz = (2 * kz == nz) ? (T)0 : kfac<T>(g.kzu, kz);
+    C2<T> ph[R2];
+    if (s1) {
+#pragma unroll
+      for (int n2 = 0; n2 < R2; ++n2) {
+        const C2<T> v = bc[(n1 + R1 * n2) * B + b];
+        ph[n2] = mk2<T>(v.x * invN, v.y * invN);
+      }
+    }
+    for (int a = 0; a < 4; ++a) {
+      __syncthreads();  // the tile (a = 0) or the last exchange has been read
+      if (s1) {
+        C2<T> v[R2];
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2) {
+          const int i = n1 + R1 * n2;
+          const C2<T> pre = ph[n2];
+          T f;
+          if (a == 0) {
+            f = (2 * i == nx) ? (T)0 : kfac<T>(g.kxu, (i > nx / 2) ? (i - nx) : i);
+          } else if (a == 1) {
+            f = fy;
+          } else if (a == 2) {
+            f = fz;
+          } else {
+            f = ksq<T>(g, (i > nx / 2) ? (nx - i) : i, ja, kz);
+          }
+          v[n2] = (a < 3) ? mk2<T>(-pre.y * f, pre.x * f)    // pre * I * k
+                          : mk2<T>(-pre.x * f, -pre.y * f);  // -pre * k^2
+        }
+        reg_dft<T, R2>(v, tw, L / R2, +1);
+#pragma unroll
+        for (int k2 = 0; k2 < R2; ++k2)
+          bc[(n1 * R2 + k2) * B + b] = (k2 == 0) ? v[k2] : cmul(v[k2], twid(tw, (n1 * k2) & (L - 1), +1));
+      }
+      __syncthreads();
+      if (tid < R2 * B) {
+        const int k2 = tid >> LB;
+        C2<T> u[R1];
+#pragma unroll
+        for (int m1 = 0; m1 < R1; ++m1) u[m1] = bc[(m1 * R2 + k2) * B + b];
+        reg_dft<T, R1>(u, tw, L / R1, +1);
+        C2<T> *o = out + a * ostride + off;
+        if (b < bv) {
+#pragma unroll
+          for (int k1 = 0; k1 < R1; ++k1) o[(long long)(k2 + R2 * k1) * sj + b] = u[k1];
+        }
+      }
+    }
+    __syncthreads();  // bc is the prefetch target of the next iteration
+  }
+  cp_async_wait<0>();
+}
+
 // energy density and pressure at one point (see above)
 template <typename T, bool MIXED>
 __device__ __forceinline__ void rho_p(T dx, T dy, T dz, T phi, T dph, T ps, T inv_a2, T m2, T third,
@@ -741,17 +1008,19 @@ __global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_z_rhs_fused(const C2<T
   const bool valid = row < rows;
   ZTw<T, H> w;
   w.load(twh, t);
-  const int b = lane_brev(t, Gm::LW);
+  C2<T> *srow = stage + (warp * Gm::G + gi) * Gm::PS;
   // the four inverse transforms: d/dx, d/dy, d/dz, laplacian of phi
   C2<T> d[4][R];
+  {
+    C2<T> wnat[R];
+    zc2r_twiddles<T, H>(twz, t, wnat);
 #pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    const C2<T> *src = d4 + a * dstride + row * (H + 1);
-#pragma unroll
-    for (int k1 = 0; k1 < R; ++k1) d[a][k1] = valid ? zc2r_pre<T>(src, k1 + R * b, H, twz) : mk2<T>(0, 0);
+    for (int a = 0; a < 4; ++a) {
+      zc2r_load<T, H>(d4 + a * dstride + row * (H + 1), t, lane & ~(W - 1), valid, wnat, d[a]);
+      zfft_dif<+1, T, H>(d[a], w, twh);
+      zunscramble<T, H>(d[a], t, srow);
+    }
   }
-#pragma unroll
-  for (int a = 0; a < 4; ++a) zfft_dit<+1, T, H>(d[a], w, twh);
   // pointwise, natural map: register n holds reals 2j, 2j+1 of j = t + W n
   const long long N = g.N;
   const double a_sc = ysc[4];
@@ -803,7 +1072,8 @@ __global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_z_rhs_fused(const C2<T
   }
   if (!gw) return;
   // the six GW source products d_i phi d_j phi, forward transforms
-  C2<T> *srow = stage + (warp * Gm::G + gi) * Gm::PS;
+  C2<T> wzl[R];
+  zr2c_twiddles<T, H>(twz, t, wzl);
 #pragma unroll 1
   for (int pr = 0; pr < 6; ++pr) {
     const int ia = pr < 3 ? 0 : (pr < 5 ? 1 : 2);
@@ -817,7 +1087,7 @@ __global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_z_rhs_fused(const C2<T
     }
     zfft_dif<-1, T, H>(u, w, twh);
     C2<T> xH;
-    zr2c_post_lanes<T, H>(u, t, lane & ~(W - 1), twz, xH);
+    zr2c_post_lanes<T, H>(u, t, lane & ~(W - 1), wzl, xH);
     C2<T> *dst = (pr < 4 ? s6 + pr * sstride4 : s6b + (pr - 4) * sstride4) + row * (H + 1);
     zstore_row<T, H>(u, xH, t, srow, dst, valid);
   }
@@ -828,6 +1098,30 @@ __global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_z_rhs_fused(const C2<T
 
 // rows of a z-pass CTA
 template <typename T, int H> constexpr int zrows() { return zwarps<T>() * ZGeo<H>::G; }
+
+// CTAs of a grid-stride kernel: at most the CTAs resident on the device at
+// once (the occupancy of the kernel, looked up once per kernel), at least one
+static unsigned resident_grid(const void *kernel, int nt, size_t smem, int num_sms,
+                              long long work) {
+  static std::mutex mu;
+  static std::unordered_map<const void *, int> occ_of;
+  int occ = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = occ_of.find(kernel);
+    if (it != occ_of.end()) {
+      occ = it->second;
+    } else {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, nt, smem) != cudaSuccess ||
+          occ < 1)
+        occ = 1;
+      occ_of[kernel] = occ;
+    }
+  }
+  const long long cap = (long long)occ * (num_sms > 0 ? num_sms : 1);
+  const long long g = work < cap ? work : cap;
+  return (unsigned)(g < 1 ? 1 : g);
+}
 
 template <typename T>
 static const C2<T> *tab(void *p) {
@@ -886,6 +1180,27 @@ struct XYLaunch {
                                                                          c->g.mz, sign, tw);
     return IH_OK;
   }
+  template <int L, int B>
+  int run_pipe(long long sj, long long so, int outer, const C2<T> *tw) {
+    const Geom &g = c->g;
+    const size_t sm = sizeof(C2<T>) * ((size_t)L + 2 * (size_t)L * B);
+    const int nt = pass_threads<L, B>();
+    static int occ = 0;  // resident CTAs per SM (a property of the kernel)
+    if (!occ) {
+      cudaFuncSetAttribute(k_fft_xy_pipe<T, L, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sm);
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fft_xy_pipe<T, L, B>, nt, sm) !=
+              cudaSuccess ||
+          occ < 1)
+        occ = 1;
+    }
+    XYTiles tl{stride, so, g.mz, (g.mz + B - 1) / B, outer};
+    const long long total = (long long)tl.ntz * outer * count;
+    const long long cap = (long long)occ * c->num_sms;
+    const unsigned nb = (unsigned)(total < cap ? total : cap);
+    k_fft_xy_pipe<T, L, B><<<nb, nt, sm, c->stream>>>(data, sj, tl, total, sign, tw);
+    return IH_OK;
+  }
   template <int L>
   int run() {
     if constexpr (L == 512 && !allow512<T>()) {
@@ -897,6 +1212,7 @@ struct XYLaunch {
       const long long so = axis == 0 ? g.mz : (long long)g.ny * g.mz;
       const int outer = axis == 0 ? g.ny : g.nx;
       const C2<T> *tw = tab<T>(axis == 0 ? c->tw_x : c->tw_y);
+      if (var == FV_PIPELINED) return run_pipe<L, B>(sj, so, outer, tw);
       const int bw = var == FV_TWOSTEP_HALF ? B / 2 : B;
       dim3 grid((g.mz + bw - 1) / bw, outer, count);
       if (var == FV_TWOSTEP) return run_2s<L, B>(grid, sj, so, tw);
@@ -934,7 +1250,9 @@ struct ZLaunch {
       constexpr int RB = zrows<T, H>();
       const Geom &g = c->g;
       const long long rows = (long long)g.nx * g.ny;
-      dim3 grid((unsigned)((rows + RB - 1) / RB), count, 1);
+      const long long groups = (rows + RB - 1) / RB;
+      const void *kf = forward ? (const void *)k_fft_zr2c<T, H> : (const void *)k_fft_zc2r<T, H>;
+      dim3 grid(resident_grid(kf, 32 * zwarps<T>(), 0, c->num_sms, groups), count, 1);
       const int nt = 32 * zwarps<T>();
       if (forward) {
         k_fft_zr2c<T, H><<<grid, nt, 0, c->stream>>>((const T *)in, istride, (C2<T> *)out, ostride,
@@ -1003,12 +1321,35 @@ struct D4Launch {
         phihat, out, out_stride, g, tab<T>(c->tw_x));
     return IH_OK;
   }
+  template <int L, int B>
+  int run_pipe() {
+    const Geom &g = c->g;
+    const size_t sm = sizeof(C2<T>) * ((size_t)L + 2 * (size_t)L * B);
+    const int nt = pass_threads<L, B>();
+    static int occ = 0;
+    if (!occ) {
+      cudaFuncSetAttribute(k_fft_x_deriv4_pipe<T, L, B>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fft_x_deriv4_pipe<T, L, B>, nt,
+                                                        sm) != cudaSuccess ||
+          occ < 1)
+        occ = 1;
+    }
+    XYTiles tl{0, g.mz, g.mz, (g.mz + B - 1) / B, g.ny};
+    const long long total = (long long)tl.ntz * g.ny;
+    const long long cap = (long long)occ * c->num_sms;
+    const unsigned nb = (unsigned)(total < cap ? total : cap);
+    k_fft_x_deriv4_pipe<T, L, B><<<nb, nt, sm, c->stream>>>(phihat, out, out_stride, tl, total, g,
+                                                            tab<T>(c->tw_x));
+    return IH_OK;
+  }
   template <int L>
   int run() {
     if constexpr (L == 512 && !allow512<T>()) {
       return IH_ERR_ARG;
     } else {
       constexpr int B = tileB<T>();
+      if (var == FV_PIPELINED) return run_pipe<L, B>();
       if (var == FV_TWOSTEP) return run_2s<L, B>();
       if (var == FV_TWOSTEP_HALF) return run_2s<L, B / 2>();
       const Geom &g = c->g;
@@ -1128,7 +1469,8 @@ int fft_tables(Ctx *c) {
 // with CUDA events on the context stream over zeroed scratch spectra; the
 // fastest is kept.  Transform timing does not depend on the data.
 static const char *variant_name(int v) {
-  return v == FV_STOCKHAM ? "stockham" : (v == FV_TWOSTEP ? "two-step" : "two-step-half");
+  static const char *names[FV_COUNT] = {"stockham", "two-step", "two-step-half", "pipelined"};
+  return (v >= 0 && v < FV_COUNT) ? names[v] : "unknown";
 }
 
 template <typename T>

@@ -100,6 +100,7 @@ struct Ctx {
   int mixed = 0;                // IH_PREC_MIXED
   size_t tsize = 8;             // sizeof(T)
   cudaStream_t stream = nullptr;
+  int num_sms = 0;              // multiprocessors of the device
   std::string err;
   size_t dev_bytes = 0;
   unsigned long long calls_rhs = 0;
@@ -166,6 +167,7 @@ enum FftVariant {
   FV_STOCKHAM = 0,      // shared-memory Stockham, tile of one 128-byte line of pencils
   FV_TWOSTEP = 1,       // register two-step, tile of one 128-byte line
   FV_TWOSTEP_HALF = 2,  // register two-step, tile of half a line
+  FV_PIPELINED = 3,     // register two-step, persistent CTAs, cp.async double buffering
   FV_COUNT
 };
 

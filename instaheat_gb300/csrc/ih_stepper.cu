@@ -212,29 +212,36 @@ struct FinalArgs {
   double *diag;               // per-segment sums [phi, dphi, psi, dpsi, h, dh] x (e5, e3), or null
 };
 
-template <typename T>
-__global__ void k_dopri_final(const T *__restrict__ y, const double *ysc, T *__restrict__ ynew,
+// The final combination and both embedded error sums in one pass
+// (dopri853.c:436-458, error() 469-486).  The FP64 homogeneous parts of the
+// three combinations are formed once per CTA in shared memory; per element
+// the work is FP32 (mixed form, rounding floor removed) or FP64, and the
+// squared ratios are accumulated in FP64 per thread.
+template <typename T, bool DIAG>
+__global__ void __launch_bounds__(256) k_dopri_final(const T *__restrict__ y, const double *ysc, T *__restrict__ ynew,
                               double *ynsc, FinalArgs a, long long N, long long nf,
                               double *partials) {
   constexpr int W = Vec4<T>::W;
   const long long nv = nf / W;
-  // homogeneous parts of the three combinations (every thread, FP64)
-  double sb[5], s5[5], s3[5], ysv[5], ynv[5];
-#pragma unroll
-  for (int s = 0; s < 5; ++s) {
+  // homogeneous parts: sb, s5, s3, y, ynew of the 5 FP64 scalars
+  __shared__ double hs[5][5];
+  if (threadIdx.x < 5) {
+    const int sidx = threadIdx.x;
     double x = 0.0, e5 = 0.0, e3 = 0.0;
+#pragma unroll
     for (int j = 0; j < 8; ++j) {
-      const double kv = a.ksc[j][s];
+      const double kv = a.ksc[j][sidx];
       x += a.b[j] * kv;
       e5 += a.e5[j] * kv;
       e3 += a.e3[j] * kv;
     }
-    sb[s] = x;
-    s5[s] = e5;
-    s3[s] = e3;
-    ysv[s] = ysc[s];
-    ynv[s] = ysc[s] + a.dt * x;
+    hs[0][sidx] = x;
+    hs[1][sidx] = e5;
+    hs[2][sidx] = e3;
+    hs[3][sidx] = ysc[sidx];
+    hs[4][sidx] = ysc[sidx] + a.dt * x;
   }
+  __syncthreads();
   T cb[8], c5[8], c3[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
@@ -243,9 +250,12 @@ __global__ void k_dopri_final(const T *__restrict__ y, const double *ysc, T *__r
     c3[j] = (T)a.e3[j];
   }
   const T dtT = (T)a.dt;
+  const T atolT = (T)a.atol, rtolT = (T)a.rtol;
+  const long long N2 = 2 * N, N3 = 3 * N, N4 = 4 * N, Nh = 4 * N + 2 * a.next;
   double err = 0.0, err2 = 0.0;
-  double dacc[12];  // per-segment error sums (diagnostic mode only)
-  for (int i = 0; i < 12; ++i) dacc[i] = 0.0;
+  double dacc[DIAG ? 12 : 1];
+#pragma unroll
+  for (int i = 0; i < (DIAG ? 12 : 1); ++i) dacc[i] = 0.0;
   for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
        v += (long long)gridDim.x * blockDim.x) {
     T ab[W], a5[W], a3[W], t5[W], t3[W], x[W];
@@ -271,59 +281,66 @@ __global__ void k_dopri_final(const T *__restrict__ y, const double *ysc, T *__r
     for (int w = 0; w < W; ++w) yn[w] = yv[w] + dtT * ab[w];
     vstore<T>(ynew + v * W, yn);
     const long long i0 = v * W;
-    const int seg = i0 < 4 * N ? (int)(i0 / N) : 4;  // W divides N: one segment per vector
+    // W divides N: a vector lies in one segment
+    const int seg = i0 < N ? 0 : (i0 < N2 ? 1 : (i0 < N3 ? 2 : (i0 < N4 ? 3 : 4)));
+    double acc5d, acc3d;
     if constexpr (sizeof(T) == 4) {
-      // mixed form: per-element arithmetic in FP32, FP32 rounding floor
-      // removed, sums of squares accumulated in FP64
+      // mixed form: per-element arithmetic in FP32, FP32 rounding floor removed
       const float nz = (float)a.noise;
-      const float ys = seg < 4 ? (float)ysv[seg] : 0.f, yns = seg < 4 ? (float)ynv[seg] : 0.f;
-      const float q5s = seg < 4 ? (float)s5[seg] : 0.f, q3s = seg < 4 ? (float)s3[seg] : 0.f;
+      const float ys = seg < 4 ? (float)hs[3][seg] : 0.f, yns = seg < 4 ? (float)hs[4][seg] : 0.f;
+      const float q5s = seg < 4 ? (float)hs[1][seg] : 0.f, q3s = seg < 4 ? (float)hs[2][seg] : 0.f;
       float acc5 = 0.f, acc3 = 0.f;
 #pragma unroll
       for (int w = 0; w < W; ++w) {
-        float f5 = fmaxf(fabsf(a5[w]) - nz * t5[w], 0.f);
-        float f3 = fmaxf(fabsf(a3[w]) - nz * t3[w], 0.f);
-        float q5 = copysignf(f5, a5[w]) + q5s, q3 = copysignf(f3, a3[w]) + q3s;
-        float sk = (float)a.atol + (float)a.rtol * fmaxf(fabsf(ys + yv[w]), fabsf(yns + yn[w]));
-        float r5 = q5 / sk, r3 = q3 / sk;
+        const float f5 = fmaxf(fabsf(a5[w]) - nz * t5[w], 0.f);
+        const float f3 = fmaxf(fabsf(a3[w]) - nz * t3[w], 0.f);
+        const float q5 = copysignf(f5, a5[w]) + q5s, q3 = copysignf(f3, a3[w]) + q3s;
+        const float isk = __frcp_rn(atolT + rtolT * fmaxf(fabsf(ys + yv[w]), fabsf(yns + yn[w])));
+        const float r5 = q5 * isk, r3 = q3 * isk;
         acc5 += r5 * r5;
         acc3 += r3 * r3;
       }
-      err2 += (double)acc5;
-      err += (double)acc3;
-      if (a.diag) {
-        const int cls = seg < 4 ? seg : (i0 < 4 * N + 2 * a.next ? 4 : 5);
-        dacc[2 * cls] += (double)acc5;
-        dacc[2 * cls + 1] += (double)acc3;
-      }
+      acc5d = (double)acc5;
+      acc3d = (double)acc3;
     } else {
-      double v5 = 0.0, v3 = 0.0;
+      const double ys = seg < 4 ? hs[3][seg] : 0.0, yns = seg < 4 ? hs[4][seg] : 0.0;
+      const double q5s = seg < 4 ? hs[1][seg] : 0.0, q3s = seg < 4 ? hs[2][seg] : 0.0;
+      acc5d = 0.0;
+      acc3d = 0.0;
 #pragma unroll
       for (int w = 0; w < W; ++w) {
-        double yf = (double)yv[w], ynf = (double)yn[w], q5 = (double)a5[w], q3 = (double)a3[w];
-        if (seg < 4) {
-          yf += ysv[seg];
-          ynf += ynv[seg];
-          q5 += s5[seg];
-          q3 += s3[seg];
-        }
-        const double sk = a.atol + a.rtol * fmax(fabs(yf), fabs(ynf));
+        const double q5 = (double)a5[w] + q5s, q3 = (double)a3[w] + q3s;
+        const double sk = a.atol + a.rtol * fmax(fabs((double)yv[w] + ys), fabs((double)yn[w] + yns));
         const double r5 = q5 / sk, r3 = q3 / sk;
-        v5 += r5 * r5;
-        v3 += r3 * r3;
+        acc5d += r5 * r5;
+        acc3d += r3 * r3;
       }
-      err2 += v5;
-      err += v3;
-      if (a.diag) {
-        const int cls = seg < 4 ? seg : (i0 < 4 * N + 2 * a.next ? 4 : 5);
-        dacc[2 * cls] += v5;
-        dacc[2 * cls + 1] += v3;
+    }
+    err2 += acc5d;
+    err += acc3d;
+    if constexpr (DIAG) {
+      const int cls = seg < 4 ? seg : (i0 < Nh ? 4 : 5);
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        if (q == cls) {
+          dacc[2 * q] += acc5d;
+          dacc[2 * q + 1] += acc3d;
+        }
       }
     }
   }
-  if (a.diag) {
+  if constexpr (DIAG) {
+#pragma unroll
     for (int i = 0; i < 12; ++i)
       if (dacc[i] != 0.0) atomicAdd(&a.diag[i], dacc[i]);
+  }
+  double ysv[5], ynv[5], s5[5], s3[5];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    ysv[q] = hs[3][q];
+    ynv[q] = hs[4][q];
+    s5[q] = hs[1][q];
+    s3[q] = hs[2][q];
   }
   // scale factor a (the last state component)
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -535,14 +552,15 @@ static int try_step(Ctx *c, double dt, double *err_out, double *rho_mean_out, in
   const int W = c->mixed ? 4 : 2;
   const unsigned nb = stream_grid(nf / W);
   prof_begin(c, KK_DOPRI_FINAL);
-  if (c->mixed)
-    k_dopri_final<float><<<nb, 256, 0, c->stream>>>((const float *)c->y.fl, c->y.sc,
-                                                    (float *)c->ynew.fl, c->ynew.sc, f, c->g.N,
-                                                    nf, c->partials);
-  else
-    k_dopri_final<double><<<nb, 256, 0, c->stream>>>((const double *)c->y.fl, c->y.sc,
-                                                     (double *)c->ynew.fl, c->ynew.sc, f,
-                                                     c->g.N, nf, c->partials);
+  if (c->mixed) {
+    auto kf = f.diag ? k_dopri_final<float, true> : k_dopri_final<float, false>;
+    kf<<<nb, 256, 0, c->stream>>>((const float *)c->y.fl, c->y.sc, (float *)c->ynew.fl, c->ynew.sc,
+                                  f, c->g.N, nf, c->partials);
+  } else {
+    auto kd = f.diag ? k_dopri_final<double, true> : k_dopri_final<double, false>;
+    kd<<<nb, 256, 0, c->stream>>>((const double *)c->y.fl, c->y.sc, (double *)c->ynew.fl,
+                                  c->ynew.sc, f, c->g.N, nf, c->partials);
+  }
   prof_end(c, KK_DOPRI_FINAL, 10.0 * nf * c->tsize);
   IH_TRY(check_launch(c, "k_dopri_final"));
   k_dopri_err_finish<<<1, 256, 0, c->stream>>>(c->partials, (int)nb, dt, (double)c->g.Ntot, c->rs,

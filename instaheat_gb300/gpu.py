@@ -19,7 +19,7 @@ from . import build as _build
 
 PREC_F64 = 0
 PREC_MIXED = 1
-FFT_STOCKHAM, FFT_TWOSTEP, FFT_TWOSTEP_HALF = 0, 1, 2
+FFT_STOCKHAM, FFT_TWOSTEP, FFT_TWOSTEP_HALF, FFT_PIPELINED = 0, 1, 2, 3
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed",
           4: "call out of order", 5: "step size underflow", 6: "non-finite value"}
@@ -312,6 +312,10 @@ class Context:
     def autotune(self):
         """Time the FFT engine variants on the device and keep the fastest."""
         self._ck(self.L_.ih_autotune(self.h), "ih_autotune")
+        return self.L_.ih_autotune_report(self.h).decode()
+
+    @property
+    def autotune_report(self):
         return self.L_.ih_autotune_report(self.h).decode()
 
     def set_engine(self, pass_, engine):

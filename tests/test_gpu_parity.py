@@ -220,7 +220,7 @@ def test_mean_dev_matches_numpy(gpu_mod):
     assert abs(out.item() - ref) <= 1e-13 * abs(ref)
 
 
-ENGINES = [0, 1, 2]  # Stockham, two-step (128-byte tiles), two-step (64-byte tiles)
+ENGINES = [0, 1, 2, 3]  # Stockham, two-step (128-byte tiles), two-step (64-byte tiles), pipelined
 
 
 @pytest.mark.parametrize("engine", ENGINES)
