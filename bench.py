@@ -142,7 +142,7 @@ class Clocks:
                 "samples": len(sm)}
 
 
-ENGINE_NAMES = {0: "stockham", 1: "two-step", 2: "two-step-half", 3: "pipelined"}
+ENGINE_NAMES = {0: "stockham", 1: "two-step", 2: "two-step-half", 3: "pipelined", 4: "three-step"}
 
 
 def make_context(gpu, precision, device):
@@ -182,8 +182,6 @@ def bench_form(gpu, precision, device, seed, steps, warmup, profile=False, clock
     ctx.sync()
     if dist:
         dist.barrier()
-    if profile:
-        ctx.profile(True)
     if clocks:
         clocks.start()
     launches0 = ctx.kernel_launches
@@ -192,8 +190,13 @@ def bench_form(gpu, precision, device, seed, steps, warmup, profile=False, clock
     ms = ctx.timer_stop()
     launches = ctx.kernel_launches - launches0
     clk = clocks.stop() if clocks else None
-    kern = ctx.profile_kernels() if profile else None
+    kern = None
     if profile:
+        # per-kernel CUDA-event timing over further steps (kernel by kernel:
+        # the timed steps above replay each DOPRI853 try as one CUDA graph)
+        ctx.profile(True)
+        dt, _ = run_steps(ctx, dt, steps)
+        kern = ctx.profile_kernels()
         ctx.profile(False)
     res = {"ms": ms, "mt": mt, "dt_next": dt, "launches": launches, "kernels": kern, "clocks": clk,
            "t": ctx.t, "device_bytes": ctx.device_bytes,

@@ -181,12 +181,23 @@ int ih_autotune(ih_context *c);
 const char *ih_autotune_report(const ih_context *c);
 /* Pin or read the engine of one pass: pass 0 = x, 1 = y, 2 = the fused
  * inverse x pass; engine IH_FFT_STOCKHAM, IH_FFT_TWOSTEP (register two-step,
- * 128-byte tiles), IH_FFT_TWOSTEP_HALF (64-byte tiles) or IH_FFT_PIPELINED
+ * 128-byte tiles), IH_FFT_TWOSTEP_HALF (64-byte tiles), IH_FFT_PIPELINED
  * (register two-step in persistent CTAs that copy the next tile in with
- * cp.async while transforming the current one). */
-enum { IH_FFT_STOCKHAM = 0, IH_FFT_TWOSTEP = 1, IH_FFT_TWOSTEP_HALF = 2, IH_FFT_PIPELINED = 3 };
+ * cp.async while transforming the current one) or IH_FFT_THREESTEP (three
+ * register steps of at most 8 values; passes 0 and 1 only). */
+enum { IH_FFT_STOCKHAM = 0, IH_FFT_TWOSTEP = 1, IH_FFT_TWOSTEP_HALF = 2, IH_FFT_PIPELINED = 3,
+       IH_FFT_THREESTEP = 4 };
 int ih_fft_set_engine(ih_context *c, int pass, int engine);
 int ih_fft_get_engine(const ih_context *c, int pass);
+
+/* CUDA graphs (no reference counterpart): each DOPRI853 try (its 11 stage
+ * combinations and RHS evaluations, the final combination and the error
+ * reduction) and each filtered post-step RHS without diagnostics is captured
+ * once per combination of the vectors it touches and replayed as one graph
+ * launch; the step size is read from device memory.  On by default; off
+ * while per-kernel timing (ih_profile_enable) or the error breakdown is on.
+ * Results are identical either way. */
+int ih_graphs_enable(ih_context *c, int on);
 
 /* ---- transforms (fft / ifft, toolbox.c:806-827) on host buffers ----
  * r2c unnormalised exp(-i..) [x][y][z/2+1]; c2r unnormalised exp(+i..).

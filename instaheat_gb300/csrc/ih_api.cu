@@ -180,6 +180,7 @@ static int create(const ih_params *p, Ctx *c) {
   c->hpin_bytes = 4096;
   IH_CUDA(c, cudaMallocHost((void **)&c->hpin, c->hpin_bytes));
   IH_TRY(dmalloc(c, &c->stage_dev, sizeof(double) * (size_t)g.Ntot));
+  IH_TRY(dmalloc(c, (void **)&c->dt_dev, sizeof(double)));
   IH_TRY(alloc_vec(c, c->y));
   IH_TRY(alloc_vec(c, c->ynew));
   IH_TRY(alloc_vec(c, c->ytmp));
@@ -204,6 +205,10 @@ static void destroy(Ctx *c) {
   if (c->hpin) cudaFreeHost(c->hpin);
   if (c->stage_dev) cudaFree(c->stage_dev);
   if (c->feat_dev) cudaFree(c->feat_dev);
+  if (c->dt_dev) cudaFree(c->dt_dev);
+  for (auto &gr : c->graphs)
+    if (gr.exec) cudaGraphExecDestroy(gr.exec);
+  c->graphs.clear();
   free_vec(c->y);
   free_vec(c->ynew);
   free_vec(c->ytmp);
@@ -469,6 +474,7 @@ int ih_autotune(ih_context *h) {
   CTX_CHECK(h);
   Ctx *c = &h->c;
   IH_TRY(fft_autotune(c));
+  c->graph_epoch += 1;
   IH_CUDA(c, cudaStreamSynchronize(c->stream));
   return IH_OK;
 }
@@ -480,11 +486,19 @@ const char *ih_autotune_report(const ih_context *h) {
 int ih_fft_set_engine(ih_context *h, int pass, int engine) {
   CTX_CHECK(h);
   if (pass < 0 || pass > 2 || engine < 0 || engine >= FV_COUNT) return IH_ERR_ARG;
+  if (pass == 2 && engine == FV_THREESTEP) return IH_ERR_ARG;
   if (pass < 2) {
     h->c.xy_var[pass] = engine;
   } else {
     h->c.d4_var = engine;
   }
+  h->c.graph_epoch += 1;
+  return IH_OK;
+}
+
+int ih_graphs_enable(ih_context *h, int on) {
+  CTX_CHECK(h);
+  h->c.graphs_on = on ? 1 : 0;
   return IH_OK;
 }
 
@@ -560,6 +574,7 @@ int ih_dopri853_init_ex(ih_context *h, const ih_dopri_cfg *cfg, double t0, doubl
     return IH_ERR_STATE;
   }
   IH_TRY(dopri_init(c, cfg, t0, dt0, want_output ? 1 : 0));
+  c->graph_epoch += 1;  // the tolerances are baked into the captured try
   IH_CUDA(c, cudaStreamSynchronize(c->stream));
   return IH_OK;
 }
@@ -777,6 +792,7 @@ int ih_dopri853_set_noise_floor(ih_context *h, double eta) {
   CTX_CHECK(h);
   if (!(eta >= 0.0)) return IH_ERR_ARG;
   h->c.noise_eta = eta;
+  h->c.graph_epoch += 1;
   return IH_OK;
 }
 

@@ -328,6 +328,80 @@ __global__ void __launch_bounds__(pass_threads<L, B>()) k_fft_xy_2s(C2<T> *data,
 }
 
 // ---------------------------------------------------------------------------
+// Three-step engine: L = R1 R2 with R2 <= 8 held per thread, and the R1-point
+// DFTs of step 2 themselves split as R1 = Ra Rb, so no thread holds more than
+// 8 values and twice as many warps fit on an SM as with the two-step engine.
+//   step 1 : thread (b, n1) DFT_R2 over x[n1 + R1 n2], twiddle w_L^(n1 k2)
+//   step 2a: thread (b, k2, m1) DFT_Rb over E1[m1 + Ra m2][k2],
+//            twiddle w_R1^(m1 j2)
+//   step 2b: thread (b, k2, j2) DFT_Ra over m1 -> X[k2 + R2 (j2 + Rb j1)]
+// One tile buffer [L][B] (rows of one line) holds both exchanges.
+template <int L> struct Fac3;
+template <> struct Fac3<64> { static constexpr int R2 = 8, Ra = 2, Rb = 4; };
+template <> struct Fac3<128> { static constexpr int R2 = 8, Ra = 4, Rb = 4; };
+template <> struct Fac3<256> { static constexpr int R2 = 8, Ra = 4, Rb = 8; };
+template <> struct Fac3<512> { static constexpr int R2 = 8, Ra = 8, Rb = 8; };
+template <int L, int B> __host__ __device__ constexpr int threads3() {
+  return (L / Fac3<L>::R2 > Fac3<L>::R2 * Fac3<L>::Ra ? L / Fac3<L>::R2 : Fac3<L>::R2 * Fac3<L>::Ra) *
+         B;
+}
+
+template <typename T, int L, int B>
+__global__ void __launch_bounds__(threads3<L, B>()) k_fft_xy_3s(C2<T> *data, long long astride, long long sj, long long so, int mz,
+                         int sign, const C2<T> *twg) {
+  constexpr int R2 = Fac3<L>::R2, Ra = Fac3<L>::Ra, Rb = Fac3<L>::Rb, R1 = Ra * Rb;
+  constexpr int LB = clog2(B);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<T> *tw = reinterpret_cast<C2<T> *>(smraw);
+  C2<T> *e = tw + L;  // [L][B]
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int z0 = blockIdx.x * B;
+  const int bv = min(B, mz - z0);
+  C2<T> *base = data + blockIdx.z * astride + (long long)blockIdx.y * so + z0;
+  load_table(tw, twg, L, tid, nt);
+  __syncthreads();
+  const int b = tid & (B - 1), q = tid >> LB;
+  if (q < R1) {  // step 1: q = n1
+    C2<T> v[R2];
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2)
+      v[n2] = (b < bv) ? base[(long long)(q + R1 * n2) * sj + b] : mk2<T>(0, 0);
+    reg_dft<T, R2>(v, tw, L / R2, sign);
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2)
+      e[(q * R2 + k2) * B + b] = (k2 == 0) ? v[k2] : cmul(v[k2], twid(tw, (q * k2) & (L - 1), sign));
+  }
+  __syncthreads();
+  C2<T> u[Rb];
+  const int m1 = q % Ra, k2a = q / Ra;
+  if (q < R2 * Ra) {  // step 2a: q = m1 + Ra k2
+#pragma unroll
+    for (int m2 = 0; m2 < Rb; ++m2) u[m2] = e[((m1 + Ra * m2) * R2 + k2a) * B + b];
+    reg_dft<T, Rb>(u, tw, L / Rb, sign);
+  }
+  __syncthreads();
+  if (q < R2 * Ra) {
+#pragma unroll
+    for (int j2 = 0; j2 < Rb; ++j2)
+      e[((k2a * Rb + j2) * Ra + m1) * B + b] =
+          (j2 == 0) ? u[j2] : cmul(u[j2], twid(tw, (m1 * j2 * R2) & (L - 1), sign));
+  }
+  __syncthreads();
+  // step 2b: tasks (b, j2 + Rb k2), R2 Rb of them per pencil
+  for (int task = q; task < R2 * Rb; task += nt >> LB) {
+    const int j2 = task % Rb, k2 = task / Rb;
+    C2<T> w[Ra];
+#pragma unroll
+    for (int mm = 0; mm < Ra; ++mm) w[mm] = e[((k2 * Rb + j2) * Ra + mm) * B + b];
+    reg_dft<T, Ra>(w, tw, L / Ra, sign);
+    if (b < bv) {
+#pragma unroll
+      for (int j1 = 0; j1 < Ra; ++j1) base[(long long)(k2 + R2 * (j2 + Rb * j1)) * sj + b] = w[j1];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Pipelined two-step engine: persistent CTAs walk the tiles of the pass; the
 // next tile is copied global -> shared with cp.async while the current one is
 // transformed, so every CTA keeps a whole tile of loads in flight (the plain
@@ -1201,6 +1275,14 @@ struct XYLaunch {
     k_fft_xy_pipe<T, L, B><<<nb, nt, sm, c->stream>>>(data, sj, tl, total, sign, tw);
     return IH_OK;
   }
+  template <int L, int B>
+  int run_3s(dim3 grid, long long sj, long long so, const C2<T> *tw) {
+    const size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * B);
+    cudaFuncSetAttribute(k_fft_xy_3s<T, L, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_fft_xy_3s<T, L, B><<<grid, threads3<L, B>(), sm, c->stream>>>(data, stride, sj, so, c->g.mz,
+                                                                     sign, tw);
+    return IH_OK;
+  }
   template <int L>
   int run() {
     if constexpr (L == 512 && !allow512<T>()) {
@@ -1213,6 +1295,13 @@ struct XYLaunch {
       const int outer = axis == 0 ? g.ny : g.nx;
       const C2<T> *tw = tab<T>(axis == 0 ? c->tw_x : c->tw_y);
       if (var == FV_PIPELINED) return run_pipe<L, B>(sj, so, outer, tw);
+      if (var == FV_THREESTEP) {
+        if constexpr (L >= 64) {
+          return run_3s<L, B>(dim3((g.mz + B - 1) / B, outer, count), sj, so, tw);
+        } else {  // short pencils: the two-step engine already holds <= 8 values
+          return run_2s<L, B>(dim3((g.mz + B - 1) / B, outer, count), sj, so, tw);
+        }
+      }
       const int bw = var == FV_TWOSTEP_HALF ? B / 2 : B;
       dim3 grid((g.mz + bw - 1) / bw, outer, count);
       if (var == FV_TWOSTEP) return run_2s<L, B>(grid, sj, so, tw);
@@ -1469,7 +1558,8 @@ int fft_tables(Ctx *c) {
 // with CUDA events on the context stream over zeroed scratch spectra; the
 // fastest is kept.  Transform timing does not depend on the data.
 static const char *variant_name(int v) {
-  static const char *names[FV_COUNT] = {"stockham", "two-step", "two-step-half", "pipelined"};
+  static const char *names[FV_COUNT] = {"stockham", "two-step", "two-step-half", "pipelined",
+                                        "three-step"};
   return (v >= 0 && v < FV_COUNT) ? names[v] : "unknown";
 }
 
@@ -1492,6 +1582,7 @@ static int autotune_t(Ctx *c) {
     int best = 0;
     float tbest = 0.f;
     for (int v = 0; v < FV_COUNT && st == IH_OK; ++v) {
+      if (pass == 2 && v == FV_THREESTEP) continue;  // the fused x pass has no three-step form
       if (pass < 2) {
         c->xy_var[pass] = v;
       } else {

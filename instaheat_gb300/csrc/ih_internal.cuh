@@ -29,6 +29,7 @@ constexpr double kTwoPi = 6.283185307179586476925286766559;
 constexpr double kPi = 3.141592653589793238462643383279;
 constexpr int kSc = 8;          // doubles of FP64 scalars per vector
 constexpr int kMaxPartials = 4096;
+constexpr int kDtSlot = 24;     // pinned host slot (doubles into Ctx::hpin) of the try's dt
 // Mixed form: each FP32 error-vector element is soft-thresholded by
 // eta * eps32 * sum_j |c_j k_j| before it enters the FP64 error norm.
 constexpr double kDefaultNoiseEta = 256.0;
@@ -155,6 +156,20 @@ struct Ctx {
   // last output flag results available
   int have_output = 0;
 
+  // CUDA graphs of the DOPRI853 try and of the filtered post-step RHS, one per
+  // combination of the vectors they touch (see ih_stepper.cu)
+  struct Graph {
+    int kind = 0;               // 0 try, 1 post-step RHS
+    unsigned epoch = 0;
+    const void *key[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long kernels = 0, rhs_calls = 0;
+  };
+  std::vector<Graph> graphs;
+  unsigned graph_epoch = 0;     // advanced when a captured parameter changes
+  int graphs_on = 1;
+  double *dt_dev = nullptr;     // step size of the current try (device)
+
   // FFT engines of the x/y passes (per axis) and of the fused x pass, chosen
   // by fft_autotune; Stockham with 128-byte tiles until tuned
   int xy_var[2] = {0, 0};
@@ -168,6 +183,7 @@ enum FftVariant {
   FV_TWOSTEP = 1,       // register two-step, tile of one 128-byte line
   FV_TWOSTEP_HALF = 2,  // register two-step, tile of half a line
   FV_PIPELINED = 3,     // register two-step, persistent CTAs, cp.async double buffering
+  FV_THREESTEP = 4,     // three register steps of <= 8 values (x/y passes only)
   FV_COUNT
 };
 

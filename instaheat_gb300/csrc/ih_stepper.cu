@@ -132,7 +132,8 @@ struct LinArgs {
   const double *insc[kMaxTerms];
   double coef[kMaxTerms];
   int n;
-  double scale;  // out = base + scale * sum coef_j in_j
+  double scale;            // out = base + scale * sum coef_j in_j
+  const double *scale_dev;  // if set, the scale is read from device memory
 };
 
 template <typename T> struct Vec4;
@@ -173,7 +174,8 @@ __global__ void k_lincomb(const T *__restrict__ base, const double *basesc, T *_
   T cf[kMaxTerms];
 #pragma unroll
   for (int j = 0; j < kMaxTerms; ++j) cf[j] = (T)args.coef[j];
-  const T sc = (T)args.scale;
+  const double scd = args.scale_dev ? *args.scale_dev : args.scale;
+  const T sc = (T)scd;
   for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
        v += (long long)gridDim.x * blockDim.x) {
     T acc[W], x[W];
@@ -196,7 +198,7 @@ __global__ void k_lincomb(const T *__restrict__ base, const double *basesc, T *_
     const int s = threadIdx.x;
     double acc = 0.0;
     for (int j = 0; j < args.n; ++j) acc += args.coef[j] * args.insc[j][s];
-    outsc[s] = basesc[s] + args.scale * acc;
+    outsc[s] = basesc[s] + scd * acc;
   }
 }
 
@@ -206,7 +208,8 @@ struct FinalArgs {
   const void *k[8];
   const double *ksc[8];
   double b[8], e5[8], e3[8];  // e5 = b - bhh on stages 1, 9, 12
-  double dt, rtol, atol;
+  const double *dt;           // step size (device memory)
+  double rtol, atol;
   double noise;               // eta * eps32 (mixed form), 0 for FP64
   long long next;             // Next (tensor segment length)
   double *diag;               // per-segment sums [phi, dphi, psi, dpsi, h, dh] x (e5, e3), or null
@@ -225,6 +228,7 @@ __global__ void __launch_bounds__(256) k_dopri_final(const T *__restrict__ y, co
   const long long nv = nf / W;
   // homogeneous parts: sb, s5, s3, y, ynew of the 5 FP64 scalars
   __shared__ double hs[5][5];
+  const double dt = *a.dt;
   if (threadIdx.x < 5) {
     const int sidx = threadIdx.x;
     double x = 0.0, e5 = 0.0, e3 = 0.0;
@@ -239,7 +243,7 @@ __global__ void __launch_bounds__(256) k_dopri_final(const T *__restrict__ y, co
     hs[1][sidx] = e5;
     hs[2][sidx] = e3;
     hs[3][sidx] = ysc[sidx];
-    hs[4][sidx] = ysc[sidx] + a.dt * x;
+    hs[4][sidx] = ysc[sidx] + dt * x;
   }
   __syncthreads();
   T cb[8], c5[8], c3[8];
@@ -249,7 +253,7 @@ __global__ void __launch_bounds__(256) k_dopri_final(const T *__restrict__ y, co
     c5[j] = (T)a.e5[j];
     c3[j] = (T)a.e3[j];
   }
-  const T dtT = (T)a.dt;
+  const T dtT = (T)dt;
   const T atolT = (T)a.atol, rtolT = (T)a.rtol;
   const long long N2 = 2 * N, N3 = 3 * N, N4 = 4 * N, Nh = 4 * N + 2 * a.next;
   double err = 0.0, err2 = 0.0;
@@ -377,8 +381,9 @@ __global__ void __launch_bounds__(256) k_dopri_final(const T *__restrict__ y, co
 
 // error() (dopri853.c:469-486) -> out[0]; <rho> and the NaN flag of the last
 // RHS -> out[1], out[2]
-__global__ void k_dopri_err_finish(const double *partials, int nb, double dt, double ntot,
+__global__ void k_dopri_err_finish(const double *partials, int nb, const double *dtp, double ntot,
                                    const RhsScalars *rs, double *out) {
+  const double dt = *dtp;
   double e = 0.0, e2 = 0.0;
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
     e += partials[2 * b];
@@ -507,8 +512,11 @@ int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0, int want_
 }
 
 // try_step + error (dopri853.c:331-486); returns err via *err_out
-static int try_step(Ctx *c, double dt, double *err_out, double *rho_mean_out, int *nonfinite) {
-  const double t = c->t;
+// One DOPRI853 try on the device (dopri853.c:331-458): the 11 stage
+// combinations and RHS evaluations, the final combination and the two error
+// sums, reduced into diag[48..50] (error(), <rho>, the NaN flag).  The step
+// size is read from c->dt_dev, so one capture serves every try.
+static int try_body(Ctx *c) {
   for (int s = 1; s < 12; ++s) {  // stage s+1 from stages 1..s
     LinArgs a;
     memset(&a, 0, sizeof a);
@@ -521,10 +529,10 @@ static int try_step(Ctx *c, double dt, double *err_out, double *rho_mean_out, in
       ++n;
     }
     a.n = n;
-    a.scale = dt;
+    a.scale_dev = c->dt_dev;
     IH_TRY(lincomb(c, c->y, c->ytmp, a));
-    const double ts = (s == 11) ? t + dt : t + DC[s] * dt;
-    IH_TRY(rhs(c, ts, c->ytmp, c->k[s + 1], 0, 0, nullptr));
+    // the RHS does not depend on t explicitly (toolbox.c:75-88)
+    IH_TRY(rhs(c, 0.0, c->ytmp, c->k[s + 1], 0, 0, nullptr));
   }
   FinalArgs f;
   memset(&f, 0, sizeof f);
@@ -538,7 +546,7 @@ static int try_step(Ctx *c, double dt, double *err_out, double *rho_mean_out, in
     f.e5[j] = DB[sidx] - bhh;
     f.e3[j] = DE3[sidx];
   }
-  f.dt = dt;
+  f.dt = c->dt_dev;
   f.rtol = c->cfg.rtol;
   f.atol = c->cfg.atol;
   f.noise = c->mixed ? c->noise_eta * 5.9604644775390625e-8 : 0.0;  // eta * 2^-24
@@ -563,9 +571,74 @@ static int try_step(Ctx *c, double dt, double *err_out, double *rho_mean_out, in
   }
   prof_end(c, KK_DOPRI_FINAL, 10.0 * nf * c->tsize);
   IH_TRY(check_launch(c, "k_dopri_final"));
-  k_dopri_err_finish<<<1, 256, 0, c->stream>>>(c->partials, (int)nb, dt, (double)c->g.Ntot, c->rs,
-                                               c->diag + 4 * c->g.bins + 48);
-  IH_TRY(check_launch(c, "k_dopri_err_finish"));
+  k_dopri_err_finish<<<1, 256, 0, c->stream>>>(c->partials, (int)nb, c->dt_dev, (double)c->g.Ntot,
+                                               c->rs, c->diag + 4 * c->g.bins + 48);
+  return check_launch(c, "k_dopri_err_finish");
+}
+
+// Work that is replayed as one CUDA graph per combination of the vectors it
+// touches (y, ynew and the first two stage vectors swap roles after every
+// accepted step).  Graphs are not used while per-kernel timing or the error
+// breakdown is on; any change of what a capture bakes in (tolerances, noise
+// floor, FFT engines) advances c->graph_epoch.
+static bool graphs_usable(const Ctx *c) { return c->graphs_on && !c->prof_on && !c->err_diag; }
+
+template <typename Body>
+static int replay(Ctx *c, int kind, const void *const key[4], Body body) {
+  Ctx::Graph *hit = nullptr;
+  for (auto &gr : c->graphs)
+    if (gr.kind == kind && gr.epoch == c->graph_epoch && gr.key[0] == key[0] &&
+        gr.key[1] == key[1] && gr.key[2] == key[2] && gr.key[3] == key[3])
+      hit = &gr;
+  if (!hit) {
+    const unsigned long long l0 = c->launches, r0 = c->calls_rhs;
+    IH_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+    const int st = body();
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+    const unsigned long long nk = c->launches - l0, nr = c->calls_rhs - r0;
+    c->launches = l0;
+    c->calls_rhs = r0;
+    if (st != IH_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (ee != cudaSuccess) {
+      c->err = std::string("graph capture: ") + cudaGetErrorString(ee);
+      return IH_ERR_CUDA;
+    }
+    Ctx::Graph gr;
+    gr.kind = kind;
+    gr.epoch = c->graph_epoch;
+    for (int i = 0; i < 4; ++i) gr.key[i] = key[i];
+    gr.kernels = nk;
+    gr.rhs_calls = nr;
+    const cudaError_t ie = cudaGraphInstantiate(&gr.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      c->err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie);
+      return IH_ERR_CUDA;
+    }
+    c->graphs.push_back(gr);
+    hit = &c->graphs.back();
+  }
+  IH_CUDA(c, cudaGraphLaunch(hit->exec, c->stream));
+  c->launches += hit->kernels;
+  c->calls_rhs += hit->rhs_calls;
+  return IH_OK;
+}
+
+// try_step + error (dopri853.c:331-486); returns err via *err_out
+static int try_step(Ctx *c, double dt, double *err_out, double *rho_mean_out, int *nonfinite) {
+  c->hpin[kDtSlot] = dt;
+  IH_CUDA(c, cudaMemcpyAsync(c->dt_dev, c->hpin + kDtSlot, sizeof(double), cudaMemcpyHostToDevice,
+                             c->stream));
+  if (graphs_usable(c)) {
+    const void *key[4] = {c->y.fl, c->ynew.fl, c->k[1].fl, c->ytmp.fl};
+    IH_TRY(replay(c, 0, key, [c]() { return try_body(c); }));
+  } else {
+    IH_TRY(try_body(c));
+  }
   IH_CUDA(c, cudaMemcpyAsync(c->hpin, c->diag + 4 * c->g.bins + 48, sizeof(double) * 3,
                              cudaMemcpyDeviceToHost, c->stream));
   IH_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -573,6 +646,14 @@ static int try_step(Ctx *c, double dt, double *err_out, double *rho_mean_out, in
   *rho_mean_out = c->hpin[1];
   *nonfinite = c->hpin[2] != 0.0;
   return IH_OK;
+}
+
+// the filtered post-step RHS (dopri853.c:285-293), replayed as a graph when
+// it computes no diagnostics
+static int post_step_rhs(Ctx *c, double t, int want_output) {
+  if (want_output || !graphs_usable(c)) return rhs(c, t, c->ynew, c->k[2], 1, want_output, &c->y);
+  const void *key[4] = {c->ynew.fl, c->k[2].fl, nullptr, nullptr};
+  return replay(c, 1, key, [c]() { return rhs(c, 0.0, c->ynew, c->k[2], 1, 0, &c->y); });
 }
 
 // success() (dopri853.c:505-540)
@@ -633,7 +714,7 @@ int dopri_step(Ctx *c, double dt_try, int want_output, ih_step_info *info) {
     }
   }
   // post-step RHS with the filter on (dopri853.c:285-293) into k[2], then swap
-  IH_TRY(rhs(c, c->t + dt, c->ynew, c->k[2], 1, want_output, &c->y));
+  IH_TRY(post_step_rhs(c, c->t + dt, want_output));
   Vec tmp = c->y;
   c->y = c->ynew;
   c->ynew = tmp;

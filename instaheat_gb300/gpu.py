@@ -19,7 +19,7 @@ from . import build as _build
 
 PREC_F64 = 0
 PREC_MIXED = 1
-FFT_STOCKHAM, FFT_TWOSTEP, FFT_TWOSTEP_HALF, FFT_PIPELINED = 0, 1, 2, 3
+FFT_STOCKHAM, FFT_TWOSTEP, FFT_TWOSTEP_HALF, FFT_PIPELINED, FFT_THREESTEP = 0, 1, 2, 3, 4
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed",
           4: "call out of order", 5: "step size underflow", 6: "non-finite value"}
@@ -153,6 +153,7 @@ def load(build_if_missing: bool = True):
     L.ih_autotune_report.argtypes = [vp]
     L.ih_fft_set_engine.argtypes = [vp, C.c_int, C.c_int]
     L.ih_fft_get_engine.argtypes = [vp, C.c_int]
+    L.ih_graphs_enable.argtypes = [vp, C.c_int]
     _lib = L
     return L
 
@@ -320,6 +321,10 @@ class Context:
 
     def set_engine(self, pass_, engine):
         self._ck(self.L_.ih_fft_set_engine(self.h, pass_, engine), "ih_fft_set_engine")
+
+    def graphs(self, on=True):
+        """Replay DOPRI853 tries and post-step RHS evaluations as CUDA graphs."""
+        self._ck(self.L_.ih_graphs_enable(self.h, int(on)), "ih_graphs_enable")
 
     def engines(self):
         return tuple(int(self.L_.ih_fft_get_engine(self.h, p)) for p in range(3))

@@ -99,6 +99,8 @@ def main(argv=None):
     ap.add_argument("--dt-study", default=None, help="comma-separated eta values")
     ap.add_argument("--gw-accuracy", type=float, default=0.0, help="t_end of the GW accuracy study")
     ap.add_argument("--etas", default="0,64,256", help="eta values of the GW accuracy study")
+    ap.add_argument("--engine", type=int, default=None,
+                    help="FFT engine of the x/y passes (0 Stockham .. 4 three-step)")
     args = ap.parse_args(argv)
     if args.gw_accuracy > 0:
         gw_accuracy(args.n, args.gw_accuracy, [float(x) for x in args.etas.split(",")], args.rtol)
@@ -108,6 +110,10 @@ def main(argv=None):
         return
     prec = gpu.PREC_MIXED if args.prec == "mixed" else gpu.PREC_F64
     ctx = gpu.Context(n=(args.n,) * 3, precision=prec)
+    if args.engine is not None:  # pin the x/y (and, where it exists, fused x) FFT engine
+        for p in range(3):
+            if not (p == 2 and args.engine == gpu.FFT_THREESTEP):
+                ctx.set_engine(p, args.engine)
     ctx.ic(seed=0, amp=1e-3)
     ctx.dopri_init(gpu.dopri_cfg(args.rtol, args.rtol), 0.0, 1e-3)   # one filtered RHS
     for _ in range(args.rhs):

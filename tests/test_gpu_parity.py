@@ -220,7 +220,14 @@ def test_mean_dev_matches_numpy(gpu_mod):
     assert abs(out.item() - ref) <= 1e-13 * abs(ref)
 
 
-ENGINES = [0, 1, 2, 3]  # Stockham, two-step (128-byte tiles), two-step (64-byte tiles), pipelined
+ENGINES = [0, 1, 2, 3, 4]  # Stockham, two-step, two-step (64-byte tiles), pipelined, three-step
+
+
+def pin_engine(ctx, engine):
+    """Pin every pass to the engine (the fused x pass has no three-step form)."""
+    for p in range(3):
+        if not (p == 2 and engine == 4):
+            ctx.set_engine(p, engine)
 
 
 @pytest.mark.parametrize("engine", ENGINES)
@@ -228,9 +235,8 @@ ENGINES = [0, 1, 2, 3]  # Stockham, two-step (128-byte tiles), two-step (64-byte
 def test_fft_engines_f64(gpu_mod, oracle_mod, n, engine):
     """Every x/y engine, every pencil length 8..256: FFTs within 1e-13."""
     ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
-    for p in range(3):
-        ctx.set_engine(p, engine)
-    assert ctx.engines() == (engine,) * 3
+    pin_engine(ctx, engine)
+    assert ctx.engines()[:2] == (engine,) * 2
     o = oracle_mod.Oracle(n=n)
     x = np.random.default_rng(1).standard_normal(n)
     R = o.fft(x)
@@ -243,8 +249,7 @@ def test_fft_engines_f64(gpu_mod, oracle_mod, n, engine):
 @pytest.mark.parametrize("n", [(32, 32, 32), (512, 16, 8)])
 def test_fft_engines_fp32(gpu_mod, oracle_mod, n, engine):
     ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
-    for p in range(3):
-        ctx.set_engine(p, engine)
+    pin_engine(ctx, engine)
     o = oracle_mod.Oracle(n=n)
     x = np.random.default_rng(2).standard_normal(n)
     R = o.fft(x)
@@ -258,8 +263,7 @@ def test_rhs_engines_f64_parity(gpu_mod, oracle_mod, engine):
     """The fused inverse x pass of each engine: FP64 RHS within 1e-11."""
     n = (64, 32, 32)
     ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
-    for p in range(3):
-        ctx.set_engine(p, engine)
+    pin_engine(ctx, engine)
     o = oracle_mod.Oracle(n=n)
     f = make_state(o, seed=9)
     r_ref, _ = o.rhs(f, filter=1)
@@ -309,3 +313,30 @@ def test_step_start_state_is_the_filtered_start(gpu_mod, oracle_mod):
     s0 = ctx.step_start_state()
     _, f_filt = o.rhs(f, filter=1)
     assert np.abs(s0 - f_filt).max() <= 1e-13 * np.abs(f_filt[: 4 * o.N]).max()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_graph_replay_is_identical_to_direct_launches(gpu_mod, oracle_mod, prec):
+    """DOPRI853 steps replayed as CUDA graphs give bit-identical states, step
+    sizes and counters to the same steps launched kernel by kernel."""
+    n = (32, 32, 16)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=6)
+    runs = []
+    for graphs in (True, False):
+        ctx = gpu_mod.Context(n=n, precision=prec)
+        ctx.graphs(graphs)
+        ctx.set_state(f)
+        ctx.dopri_init(gpu_mod.dopri_cfg(1e-9, 1e-9), 0.0, 5e-3)
+        dt, seq = 5e-3, []
+        c0, l0 = ctx.calls_rhs, ctx.kernel_launches
+        for _ in range(5):
+            info = ctx.dopri_step(dt)
+            seq.append((info.dt_did, info.tries, info.err))
+            dt = info.dt_next
+        runs.append((ctx.get_state(), seq, ctx.calls_rhs - c0, ctx.kernel_launches - l0))
+        ctx.close()
+    (s1, q1, c1, l1), (s2, q2, c2, l2) = runs
+    assert q1 == q2
+    assert np.array_equal(s1, s2)
+    assert c1 == c2 and l1 == l2
