@@ -280,6 +280,31 @@ int ih_step_features(ih_context *c, float *out12);
 /* set (or with NULL clear) the proposer of a context */
 int ih_dopri853_set_proposer(ih_context *c, ih_mlp *m);
 
+/* ---- ensembles (no reference counterpart: the reference runs one
+ * realization per process) ----
+ * An ensemble owns `count` member contexts (each its own grid, box and
+ * precision; powers of two as for ih_create) on one device.  Initial data
+ * and outputs go through the member contexts (ih_ensemble_member).
+ * ih_ensemble_run advances every member to tf with its own DOPRI853 step
+ * sizes and controller (each member follows exactly the step sequence that
+ * ih_dopri853_run would give it alone): in each round every unfinished
+ * member queues one try -- one CUDA-graph launch on the member's own stream
+ * -- before any is waited for, so the members' tries run concurrently;
+ * accepted members queue their filtered post-step RHS.  *rounds and *steps
+ * receive the rounds taken and the accepted steps of all members. */
+typedef struct ih_ensemble ih_ensemble;
+int ih_ensemble_create(const ih_params *members, int count, ih_ensemble **out);
+void ih_ensemble_destroy(ih_ensemble *e);
+const char *ih_ensemble_last_error(const ih_ensemble *e);
+int ih_ensemble_size(const ih_ensemble *e);
+ih_context *ih_ensemble_member(ih_ensemble *e, int i);
+/* ih_autotune once per distinct grid and precision, shared by the members */
+int ih_ensemble_autotune(ih_ensemble *e);
+int ih_ensemble_dopri_init(ih_ensemble *e, const ih_dopri_cfg *cfg, double t0,
+                           double dt0);
+int ih_ensemble_run(ih_ensemble *e, double tf, long max_rounds, long *rounds,
+                    long *steps);
+
 /* ---- RK4 (rk4.c:27-132) ---- */
 /* One step of size dt from the context time; the stage-1 RHS runs with
  * filter=1 and, if want_output, output=1 (rk4.c:63-75). */

@@ -796,4 +796,158 @@ int ih_dopri853_set_noise_floor(ih_context *h, double eta) {
   return IH_OK;
 }
 
+// ---------------------------------------------------------------------------
+// ensembles: member contexts stepped together
+struct ih_ensemble {
+  std::vector<ih_context *> m;
+  std::string err;
+};
+
+int ih_ensemble_create(const ih_params *members, int count, ih_ensemble **out) {
+  if (!out || !members || count < 1) return IH_ERR_ARG;
+  *out = nullptr;
+  ih_ensemble *e = new (std::nothrow) ih_ensemble();
+  if (!e) return IH_ERR_ALLOC;
+  for (int i = 0; i < count; ++i) {
+    ih_context *h = nullptr;
+    const int s = ih_create(&members[i], &h);
+    if (s != IH_OK) {
+      for (auto x : e->m) ih_destroy(x);
+      delete e;
+      return s;
+    }
+    e->m.push_back(h);
+  }
+  *out = e;
+  return IH_OK;
+}
+
+void ih_ensemble_destroy(ih_ensemble *e) {
+  if (!e) return;
+  for (auto x : e->m) ih_destroy(x);
+  delete e;
+}
+
+const char *ih_ensemble_last_error(const ih_ensemble *e) { return e ? e->err.c_str() : "null ensemble"; }
+int ih_ensemble_size(const ih_ensemble *e) { return e ? (int)e->m.size() : 0; }
+ih_context *ih_ensemble_member(ih_ensemble *e, int i) {
+  return (e && i >= 0 && i < (int)e->m.size()) ? e->m[i] : nullptr;
+}
+
+static int ens_fail(ih_ensemble *e, int i, int s) {
+  e->err = "member " + std::to_string(i) + ": " + ih_last_error(e->m[i]);
+  return s;
+}
+
+int ih_ensemble_autotune(ih_ensemble *e) {
+  if (!e) return IH_ERR_ARG;
+  // one tuning per distinct grid and precision, copied to the members alike
+  for (size_t i = 0; i < e->m.size(); ++i) {
+    Ctx *c = &e->m[i]->c;
+    const Ctx *twin = nullptr;
+    for (size_t j = 0; j < i; ++j) {
+      const Ctx *d = &e->m[j]->c;
+      if (d->g.nx == c->g.nx && d->g.ny == c->g.ny && d->g.nz == c->g.nz && d->mixed == c->mixed &&
+          d->p.device == c->p.device)
+        twin = d;
+    }
+    if (twin) {
+      c->xy_var[0] = twin->xy_var[0];
+      c->xy_var[1] = twin->xy_var[1];
+      c->d4_var = twin->d4_var;
+      c->tune_report = twin->tune_report;
+      c->graph_epoch += 1;
+    } else {
+      const int s = ih_autotune(e->m[i]);
+      if (s != IH_OK) return ens_fail(e, (int)i, s);
+    }
+  }
+  return IH_OK;
+}
+
+int ih_ensemble_dopri_init(ih_ensemble *e, const ih_dopri_cfg *cfg, double t0, double dt0) {
+  if (!e) return IH_ERR_ARG;
+  for (size_t i = 0; i < e->m.size(); ++i) {
+    const int s = ih_dopri853_init(e->m[i], cfg, t0, dt0);
+    if (s != IH_OK) return ens_fail(e, (int)i, s);
+  }
+  return IH_OK;
+}
+
+int ih_ensemble_run(ih_ensemble *e, double tf, long max_rounds, long *rounds_out,
+                    long *steps_out) {
+  if (!e) return IH_ERR_ARG;
+  const size_t n = e->m.size();
+  // per member: the run loop of dopri853.c:118-155 (as ih_dopri853_run), one
+  // try per round; all members' tries of a round are queued before any is
+  // waited for, so they run concurrently on the members' streams
+  std::vector<double> dt(n), dt_step(n);
+  std::vector<int> active(n), fresh(n, 1), tries(n, 0);
+  for (size_t i = 0; i < n; ++i) {
+    Ctx *c = &e->m[i]->c;
+    if (!c->dopri_ready) {
+      e->err = "member " + std::to_string(i) + ": ih_dopri853_init has not been called";
+      return IH_ERR_STATE;
+    }
+    dt[i] = c->dt_next;
+    active[i] = c->t < tf;
+  }
+  long rounds = 0, steps = 0;
+  for (; rounds < max_rounds; ++rounds) {
+    bool any = false;
+    for (size_t i = 0; i < n; ++i) {
+      if (!active[i]) continue;
+      any = true;
+      Ctx *c = &e->m[i]->c;
+      if (fresh[i]) {
+        if (c->t + dt[i] * 1.0001 > tf) dt[i] = tf - c->t;
+        dt_step[i] = dt[i];
+        fresh[i] = 0;
+        tries[i] = 0;
+      }
+      const int s = try_enqueue(c, dt[i]);
+      if (s != IH_OK) return ens_fail(e, (int)i, s);
+    }
+    if (!any) break;
+    for (size_t i = 0; i < n; ++i) {
+      if (!active[i]) continue;
+      Ctx *c = &e->m[i]->c;
+      double err, rho_mean;
+      int nonfinite;
+      int s = try_collect(c, &err, &rho_mean, &nonfinite);
+      if (s != IH_OK) return ens_fail(e, (int)i, s);
+      ++tries[i];
+      const int o = try_outcome(c, err, rho_mean, nonfinite, &dt[i]);
+      if (o < 0) return ens_fail(e, (int)i, -o);
+      if (o == 0) continue;  // retry with the reduced dt next round
+      ih_step_info info;
+      s = step_accept(c, dt[i], err, rho_mean, 0, tries[i], &info);
+      if (s != IH_OK) return ens_fail(e, (int)i, s);
+      ++steps;
+      if (info.dt_did == dt_step[i]) {
+        ++c->n_ok;
+      } else {
+        ++c->n_bad;
+      }
+      ++c->n_stp;
+      fresh[i] = 1;
+      if (c->t >= tf || fabs(c->dt_next) <= c->cfg.dt_min || (double)c->n_stp >= c->cfg.max_steps) {
+        active[i] = 0;
+      } else {
+        dt[i] = c->dt_next;
+      }
+    }
+  }
+  for (size_t i = 0; i < n; ++i) {
+    const cudaError_t ce = cudaStreamSynchronize(e->m[i]->c.stream);
+    if (ce != cudaSuccess) {
+      e->err = std::string("member stream: ") + cudaGetErrorString(ce);
+      return IH_ERR_CUDA;
+    }
+  }
+  if (rounds_out) *rounds_out = rounds;
+  if (steps_out) *steps_out = steps;
+  return IH_OK;
+}
+
 }  // extern "C"

@@ -280,6 +280,12 @@ int field_rms(Ctx *c, const void *arr, long long n, double *dev_out);
 
 // stepper (ih_stepper.cu)
 int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0, int want_output = 0);
+// pieces of perform_step for drivers that interleave several contexts
+int try_enqueue(Ctx *c, double dt);
+int try_collect(Ctx *c, double *err, double *rho_mean, int *nonfinite);
+int try_outcome(Ctx *c, double err, double rho_mean, int nonfinite, double *dt);
+int step_accept(Ctx *c, double dt, double err, double rho_mean, int want_output, int tries,
+                ih_step_info *info);
 int dopri_step(Ctx *c, double dt_try, int want_output, ih_step_info *info);
 int rk4_step(Ctx *c, double dt, int want_output);
 void dopri_tableau(double *cc, double *a, double *b, double *bhh, double *er);

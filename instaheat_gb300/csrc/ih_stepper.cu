@@ -628,8 +628,10 @@ static int replay(Ctx *c, int kind, const void *const key[4], Body body) {
   return IH_OK;
 }
 
-// try_step + error (dopri853.c:331-486); returns err via *err_out
-static int try_step(Ctx *c, double dt, double *err_out, double *rho_mean_out, int *nonfinite) {
+// try_step + error (dopri853.c:331-486) in two halves: try_enqueue queues
+// the try and the read-back of its error on the context stream and returns;
+// try_collect waits for them.
+int try_enqueue(Ctx *c, double dt) {
   c->hpin[kDtSlot] = dt;
   IH_CUDA(c, cudaMemcpyAsync(c->dt_dev, c->hpin + kDtSlot, sizeof(double), cudaMemcpyHostToDevice,
                              c->stream));
@@ -641,11 +643,20 @@ static int try_step(Ctx *c, double dt, double *err_out, double *rho_mean_out, in
   }
   IH_CUDA(c, cudaMemcpyAsync(c->hpin, c->diag + 4 * c->g.bins + 48, sizeof(double) * 3,
                              cudaMemcpyDeviceToHost, c->stream));
+  return IH_OK;
+}
+
+int try_collect(Ctx *c, double *err_out, double *rho_mean_out, int *nonfinite) {
   IH_CUDA(c, cudaStreamSynchronize(c->stream));
   *err_out = c->hpin[0];
   *rho_mean_out = c->hpin[1];
   *nonfinite = c->hpin[2] != 0.0;
   return IH_OK;
+}
+
+static int try_step(Ctx *c, double dt, double *err_out, double *rho_mean_out, int *nonfinite) {
+  IH_TRY(try_enqueue(c, dt));
+  return try_collect(c, err_out, rho_mean_out, nonfinite);
 }
 
 // the filtered post-step RHS (dopri853.c:285-293), replayed as a graph when
@@ -684,36 +695,11 @@ static int success(Ctx *c, double err, double rho_mean, double *dt) {
   return 0;
 }
 
-int dopri_step(Ctx *c, double dt_try, int want_output, ih_step_info *info) {
-  if (!c->dopri_ready) {
-    c->err = "ih_dopri853_init has not been called";
-    return IH_ERR_STATE;
-  }
-  double dt = dt_try;
-  int tries = 0;
-  double err = 0.0, rho_mean = 0.0;
-  for (;;) {
-    int nonfinite;
-    IH_TRY(try_step(c, dt, &err, &rho_mean, &nonfinite));
-    ++tries;
-    ++c->n_tries;
-    c->last_err = err;
-    if (nonfinite) {
-      c->err = "non-finite value in the RHS reductions or the error norm";
-      if (info) info->status = IH_ERR_NAN;
-      return IH_ERR_NAN;
-    }
-    if (success(c, err, rho_mean, &dt)) break;
-    if (fabs(dt) <= fabs(c->t) * DBL_EPSILON) {
-      c->err = "step size underflow";
-      if (info) {
-        info->status = IH_ERR_UNDERFLOW;
-        info->tries = tries;
-      }
-      return IH_ERR_UNDERFLOW;
-    }
-  }
-  // post-step RHS with the filter on (dopri853.c:285-293) into k[2], then swap
+// The rest of perform_step once a try is accepted (dopri853.c:285-311): the
+// filtered post-step RHS (queued), the swap of field/field_new and of the
+// stage-1 vectors, the step history and, with a proposer, its dt_next.
+int step_accept(Ctx *c, double dt, double err, double rho_mean, int want_output, int tries,
+                ih_step_info *info) {
   IH_TRY(post_step_rhs(c, c->t + dt, want_output));
   Vec tmp = c->y;
   c->y = c->ynew;
@@ -742,6 +728,48 @@ int dopri_step(Ctx *c, double dt_try, int want_output, ih_step_info *info) {
     info->status = IH_OK;
   }
   return IH_OK;
+}
+
+// bookkeeping of one finished try; returns 1 when accepted (dt is then the
+// accepted size), 0 to retry with the reduced dt, or an error status < 0
+int try_outcome(Ctx *c, double err, double rho_mean, int nonfinite, double *dt) {
+  ++c->n_tries;
+  c->last_err = err;
+  if (nonfinite) {
+    c->err = "non-finite value in the RHS reductions or the error norm";
+    return -IH_ERR_NAN;
+  }
+  if (success(c, err, rho_mean, dt)) return 1;
+  if (fabs(*dt) <= fabs(c->t) * DBL_EPSILON) {
+    c->err = "step size underflow";
+    return -IH_ERR_UNDERFLOW;
+  }
+  return 0;
+}
+
+int dopri_step(Ctx *c, double dt_try, int want_output, ih_step_info *info) {
+  if (!c->dopri_ready) {
+    c->err = "ih_dopri853_init has not been called";
+    return IH_ERR_STATE;
+  }
+  double dt = dt_try;
+  int tries = 0;
+  double err = 0.0, rho_mean = 0.0;
+  for (;;) {
+    int nonfinite;
+    IH_TRY(try_step(c, dt, &err, &rho_mean, &nonfinite));
+    ++tries;
+    const int o = try_outcome(c, err, rho_mean, nonfinite, &dt);
+    if (o == 1) break;
+    if (o < 0) {
+      if (info) {
+        info->status = -o;
+        info->tries = tries;
+      }
+      return -o;
+    }
+  }
+  return step_accept(c, dt, err, rho_mean, want_output, tries, info);
 }
 
 // rk4.c:108-161 (one step)

@@ -154,6 +154,18 @@ def load(build_if_missing: bool = True):
     L.ih_fft_set_engine.argtypes = [vp, C.c_int, C.c_int]
     L.ih_fft_get_engine.argtypes = [vp, C.c_int]
     L.ih_graphs_enable.argtypes = [vp, C.c_int]
+    L.ih_ensemble_create.argtypes = [C.POINTER(Params), C.c_int, C.POINTER(vp)]
+    L.ih_ensemble_destroy.argtypes = [vp]
+    L.ih_ensemble_destroy.restype = None
+    L.ih_ensemble_last_error.restype = C.c_char_p
+    L.ih_ensemble_last_error.argtypes = [vp]
+    L.ih_ensemble_size.argtypes = [vp]
+    L.ih_ensemble_member.restype = vp
+    L.ih_ensemble_member.argtypes = [vp, C.c_int]
+    L.ih_ensemble_autotune.argtypes = [vp]
+    L.ih_ensemble_dopri_init.argtypes = [vp, C.POINTER(DopriCfg), C.c_double, C.c_double]
+    L.ih_ensemble_run.argtypes = [vp, C.c_double, C.c_long, C.POINTER(C.c_long),
+                                  C.POINTER(C.c_long)]
     _lib = L
     return L
 
@@ -329,10 +341,26 @@ class Context:
     def engines(self):
         return tuple(int(self.L_.ih_fft_get_engine(self.h, p)) for p in range(3))
 
+    @classmethod
+    def _member(cls, handle, p: Params):
+        """A view of an ensemble member (the ensemble owns the context)."""
+        self = cls.__new__(cls)
+        self.L_ = load()
+        self.n = (p.nx, p.ny, p.nz)
+        self.box = (p.lx, p.ly, p.lz)
+        self.bins = p.bins
+        self.precision = p.precision
+        self.p = p
+        self.h = C.c_void_p(handle)
+        self._borrowed = True
+        self.N, self.M, self.Next, self.Ntot = sizes(p.nx, p.ny, p.nz)
+        return self
+
     # --- lifecycle ---
     def close(self):
         if getattr(self, "h", None):
-            self.L_.ih_destroy(self.h)
+            if not getattr(self, "_borrowed", False):
+                self.L_.ih_destroy(self.h)
             self.h = None
 
     def __enter__(self):
@@ -555,3 +583,60 @@ class Context:
         ms, n = C.c_double(), C.c_long()
         self._ck(self.L_.ih_profile_read(self.h, cls, C.byref(ms), C.byref(n)), "ih_profile_read")
         return ms.value, n.value
+
+
+class Ensemble:
+    """Member grids stepped together (wraps ih_ensemble).  members: list of
+    dicts with the Context keywords n, L, and optionally mass, gw, filter,
+    bins, precision."""
+
+    def __init__(self, members, device=0):
+        self.L_ = load()
+        ps = []
+        for m in members:
+            nx, ny, nz = m["n"]
+            L = tuple(float(x) for x in m.get("L", (20.0, 20.0, 20.0)))
+            ps.append(Params(nx, ny, nz, L[0], L[1], L[2], m.get("mass", 1.0), int(m.get("gw", True)),
+                             int(m.get("filter", True)), int(m.get("bins", nx // 2)),
+                             m.get("precision", PREC_MIXED), device))
+        arr = (Params * len(ps))(*ps)
+        h = C.c_void_p()
+        st = self.L_.ih_ensemble_create(arr, len(ps), C.byref(h))
+        if st:
+            raise IHError(st, "ih_ensemble_create")
+        self.h = h
+        self.members = [Context._member(self.L_.ih_ensemble_member(h, i), ps[i]) for i in range(len(ps))]
+
+    def _ck(self, st, what):
+        if st:
+            raise IHError(st, f"{what}: {self.L_.ih_ensemble_last_error(self.h).decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            for m in self.members:
+                m.h = None
+            self.L_.ih_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return len(self.members)
+
+    def autotune(self):
+        self._ck(self.L_.ih_ensemble_autotune(self.h), "ih_ensemble_autotune")
+
+    def dopri_init(self, cfg, t0=0.0, dt0=1e-3):
+        self._ck(self.L_.ih_ensemble_dopri_init(self.h, C.byref(cfg), t0, dt0),
+                 "ih_ensemble_dopri_init")
+
+    def run(self, tf, max_rounds=10 ** 9):
+        """Advance every member to tf; returns (rounds, accepted steps)."""
+        rounds, steps = C.c_long(), C.c_long()
+        self._ck(self.L_.ih_ensemble_run(self.h, tf, max_rounds, C.byref(rounds), C.byref(steps)),
+                 "ih_ensemble_run")
+        return int(rounds.value), int(steps.value)
