@@ -14,7 +14,11 @@
  * the DOPRI853 controller keys, OUTPUT_*).
  *
  * Two optional keys select the GPU form: IH_PRECISION (IH_PREC_F64, the
- * default, or IH_PREC_MIXED) and IH_DEVICE (CUDA ordinal, default 0).
+ * default, or IH_PREC_MIXED) and IH_DEVICE (CUDA ordinal, default 0).  A
+ * third, IH_OUTPUT_INTERVAL (> 0), makes run_dopri853 land steps on
+ * ti + k * IH_OUTPUT_INTERVAL and write the time slices there (as its
+ * overshoot clamp lands the last step on tf) instead of every
+ * TIME_STEP_SKIPS steps.
  *
  * Differences from the reference functions, all on the side of what callers
  * observe after a call:

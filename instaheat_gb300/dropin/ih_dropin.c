@@ -255,12 +255,26 @@ void run_dopri853()
 
     TIME(mon.integration = -get_wall_time());
     size_t n_stp, n_ok = 0, n_bad = 0;
+#ifdef IH_OUTPUT_INTERVAL
+    /* output landing: steps are shortened to end on ti + k * interval, and
+     * the slices are written there instead of every TIME_STEP_SKIPS steps */
+    size_t n_out = 1;
+    double t_out_next = pars.t.ti + (double)n_out * IH_OUTPUT_INTERVAL;
+#endif
     for (n_stp = 0;; ++n_stp) {
         if (t + dt * 1.0001 > tf) {
             dt = tf - t;
             INFO(printf("\nOvershoot, new dt = %f\n", dt));
         }
+#ifdef IH_OUTPUT_INTERVAL
+        int out = 0;
+        if (t_out_next < tf && t + dt * 1.0001 > t_out_next) {
+            dt = t_out_next - t;
+            out = 1;
+        }
+#else
         const int out = ((n_stp + 1) % pars.file.skip == 0);
+#endif
         ih_step_info info;
         const int st = ih_dopri853_step(c, dt, out, &info);
         if (st == IH_ERR_UNDERFLOW) {
@@ -278,11 +292,22 @@ void run_dopri853()
         t = info.t;
         pars.t.t = t;
         t_out.tmp[0] = t;
+#ifdef IH_OUTPUT_INTERVAL
+        /* a rejected landing try ends short of the output time: no slice */
+        if (out && fabs(t - t_out_next) <= 1e-12 * fmax(1.0, fabs(t_out_next))) {
+            IH_CHECK("run_dopri853", ih_get_state(c, field));
+            fill_outputs(c);
+            save();
+            ++n_out;
+            t_out_next = pars.t.ti + (double)n_out * IH_OUTPUT_INTERVAL;
+        }
+#else
         if (out) {
             IH_CHECK("run_dopri853", ih_get_state(c, field));
             fill_outputs(c);
             save();
         }
+#endif
         if (t >= tf) {
             puts("\nReached specified final time.\n");
             break;

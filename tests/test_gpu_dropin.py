@@ -158,3 +158,56 @@ def test_run_rk4_through_the_dropin(tmp_path, oracle_mod):
     exp, f_exp = _expected_rk4(oracle_mod, p)
     _compare_series(got, exp)
     assert np.abs(final - f_exp).max() <= 1e-9 * np.abs(f_exp[: 4 * 16 ** 3]).max()
+
+
+def _expected_landing(oracle_mod, p):
+    """run_dopri853 with output landing (IH_OUTPUT_INTERVAL) restated over the
+    oracle: steps shortened to end on multiples of the interval, slices there."""
+    n = (int(p["GRIDPOINTS_X"]),) * 3
+    o = oracle_mod.Oracle(n=n, bins=int(p["POWER_SPECTRUM_BINS"]))
+    f = _initial_state(o)
+    o.initial_psi(f)
+    cfg = oracle_mod.default_cfg(float(p["RELATIVE_TOLERANCE"]), float(p["ABSOLUTE_TOLERANCE"]),
+                                 float(p["MAX_DT_HUBBLE_FRACTION"]))
+    tf, dt = float(p["FINAL_TIME"]), float(p["DELTA_T"])
+    interval = float(p["IH_OUTPUT_INTERVAL"])
+    out = {}
+    d = oracle_mod.DiagOutput(o.bins)
+    _, f_filt = o.rhs(f, filter=1, output=1, diag=d)
+    _record(out, o, f_filt, 0.0, d, o.field_array("rho"))
+    st, df = o.dopri_init(f, cfg, 0.0, dt)
+    t, n_out = 0.0, 1
+    t_next = n_out * interval
+    while True:
+        if t + dt * 1.0001 > tf:
+            dt = tf - t
+        want = False
+        if t_next < tf and t + dt * 1.0001 > t_next:
+            dt = t_next - t
+            want = True
+        d = oracle_mod.DiagOutput(o.bins)
+        assert o.dopri_step(f, df, cfg, st, dt, d if want else None) == 0
+        t = st.t
+        if want and abs(t - t_next) <= 1e-12 * max(1.0, abs(t_next)):
+            _record(out, o, f, t, d, o.field_array("rho"))
+            n_out += 1
+            t_next = n_out * interval
+        if t >= tf:
+            break
+        dt = st.dt_next
+    saves = len(out["time"])
+    if saves % int(p["WRITE_OUT_BUFFER_NUMBER"]) != 0 and out["time"][-1][0] < t:
+        d = oracle_mod.DiagOutput(o.bins)
+        _, f = o.rhs(f, t=t, filter=1, output=1, diag=d)
+        _record(out, o, f, t, d, o.field_array("rho"))
+    return {k: np.array(v) for k, v in out.items()}
+
+
+def test_run_dopri853_output_landing(tmp_path, oracle_mod):
+    p, got, _ = _run_host(tmp_path, "parameters_landing.sh", oracle_mod)
+    exp = _expected_landing(oracle_mod, p)
+    times = got["time"][:, 0]
+    # slices at 0, 0.02 and 0.04 (landed); the third fills the buffer of three,
+    # so the wrap-up adds no slice at 0.05 (dopri853.c:209-212)
+    np.testing.assert_allclose(times, [0.0, 0.02, 0.04], atol=1e-14)
+    _compare_series(got, exp)
