@@ -319,16 +319,49 @@ class Context:
         self.h = h
         self.N, self.M, self.Next, self.Ntot = sizes(nx, ny, nz)
         if autotune:
-            self.autotune()
+            self.autotune(wisdom=True)
 
     # --- FFT engines ---
-    def autotune(self):
-        """Time the FFT engine variants on the device and keep the fastest."""
+    def autotune(self, wisdom=False):
+        """Time the FFT engine variants on the device and keep the fastest.
+
+        With wisdom=True the choice is kept in a small JSON file (like FFTW's
+        wisdom; path $IH_FFT_WISDOM, default _lib/fft_wisdom.json) keyed by
+        grid and precision, and an existing entry is reused instead of timing
+        again -- so that a later run of the same program, e.g. under a
+        profiler whose serialised launches would time the engines
+        differently, uses the same engines."""
+        import json
+        import os
+        path = Path(os.environ.get("IH_FFT_WISDOM", str(_build.OUT / "fft_wisdom.json")))
+        key = "%dx%dx%d:%d" % (self.n + (self.precision,))
+        if wisdom and path.exists():
+            try:
+                known = json.loads(path.read_text()).get(key)
+            except ValueError:
+                known = None
+            if known:
+                for p, e in enumerate(known["engines"]):
+                    self.set_engine(p, e)
+                self._wisdom_report = "from wisdom: " + known["report"]
+                return self._wisdom_report
         self._ck(self.L_.ih_autotune(self.h), "ih_autotune")
-        return self.L_.ih_autotune_report(self.h).decode()
+        report = self.L_.ih_autotune_report(self.h).decode()
+        self._wisdom_report = None
+        if wisdom:
+            try:
+                data = json.loads(path.read_text()) if path.exists() else {}
+            except ValueError:
+                data = {}
+            data[key] = {"engines": list(self.engines()), "report": report}
+            path.parent.mkdir(parents=True, exist_ok=True)
+            path.write_text(json.dumps(data))
+        return report
 
     @property
     def autotune_report(self):
+        if getattr(self, "_wisdom_report", None):
+            return self._wisdom_report
         return self.L_.ih_autotune_report(self.h).decode()
 
     def set_engine(self, pass_, engine):
