@@ -31,6 +31,7 @@
 //                       products, all on one tile of rows.
 #include <math.h>
 #include <mutex>
+#include <utility>
 #include <unordered_map>
 #include "ih_internal.cuh"
 
@@ -68,9 +69,6 @@ __device__ __forceinline__ V csub(V a, V b) {
 
 template <typename T> __host__ __device__ constexpr int tileB() { return 128 / (int)(2 * sizeof(T)); }
 __host__ __device__ constexpr int clog2(int v) { return v <= 1 ? 0 : 1 + clog2(v >> 1); }
-__host__ __device__ constexpr int brev(int x, int bits) {
-  return bits == 0 ? 0 : (((x & 1) << (bits - 1)) | brev(x >> 1, bits - 1));
-}
 
 // L = R1 * R2: threads per pencil in step 1, points per thread in step 1
 template <int L> struct Fac;
@@ -98,9 +96,41 @@ template <typename T>
 __device__ __forceinline__ C2<T> w16(int m) {
   constexpr double c = 0.92387953251128675613, s = 0.38268343236508977173,
                    h = 0.70710678118654752440;
-  constexpr double re[16] = {1, c, h, s, 0, -s, -h, -c, -1, -c, -h, -s, 0, s, h, c};
-  constexpr double im[16] = {0, -s, -h, -c, -1, -c, -h, -s, 0, s, h, c, 1, c, h, s};
-  return mk2<T>((T)re[m & 15], (T)im[m & 15]);
+  // a switch (not a table) so that a constant m folds to two literals
+  switch (m & 15) {
+    case 0: return mk2<T>((T)1, (T)0);
+    case 1: return mk2<T>((T)c, (T)-s);
+    case 2: return mk2<T>((T)h, (T)-h);
+    case 3: return mk2<T>((T)s, (T)-c);
+    case 4: return mk2<T>((T)0, (T)-1);
+    case 5: return mk2<T>((T)-s, (T)-c);
+    case 6: return mk2<T>((T)-h, (T)-h);
+    case 7: return mk2<T>((T)-c, (T)-s);
+    case 8: return mk2<T>((T)-1, (T)0);
+    case 9: return mk2<T>((T)-c, (T)s);
+    case 10: return mk2<T>((T)-h, (T)h);
+    case 11: return mk2<T>((T)-s, (T)c);
+    case 12: return mk2<T>((T)0, (T)1);
+    case 13: return mk2<T>((T)s, (T)c);
+    case 14: return mk2<T>((T)h, (T)h);
+    default: return mk2<T>((T)c, (T)s);
+  }
+}
+
+// bit reversal of K over BITS bits, as a compile-time constant
+template <int K, int BITS> struct Brev {
+  static constexpr int value = ((K & 1) << (BITS - 1)) | Brev<(K >> 1), BITS - 1>::value;
+};
+template <int K> struct Brev<K, 0> {
+  static constexpr int value = 0;
+};
+
+// v[k] <- v[brev(k)], every index a template constant (the registers are
+// renamed; nothing is staged in local memory)
+template <typename T, int R, int... K>
+__device__ __forceinline__ void brev_permute(C2<T> (&v)[R], std::integer_sequence<int, K...>) {
+  const C2<T> t[R] = {v[Brev<K, clog2(R)>::value]...};
+  ((v[K] = t[K]), ...);
 }
 
 // In-register DFT of R points: v[k] <- sum_n v[n] exp(sign 2 pi i nk/R).
@@ -132,11 +162,7 @@ __device__ __forceinline__ void reg_dft(C2<T> (&v)[R], const C2<T> *tw, int ts, 
       }
     }
   }
-  C2<T> t[R];
-#pragma unroll
-  for (int k = 0; k < R; ++k) t[k] = v[brev(k, LOGR)];
-#pragma unroll
-  for (int k = 0; k < R; ++k) v[k] = t[k];
+  brev_permute<T, R>(v, std::make_integer_sequence<int, R>{});
 }
 
 // exp(sign 2 pi i m / L) from the table exp(-2 pi i m/L)
