@@ -200,8 +200,9 @@ def bench_form(gpu, precision, device, seed, steps, warmup, profile=False, clock
         ctx.profile(False)
     res = {"ms": ms, "mt": mt, "dt_next": dt, "launches": launches, "kernels": kern, "clocks": clk,
            "t": ctx.t, "device_bytes": ctx.device_bytes,
-           "fft_engines": dict(zip(("x", "y", "deriv4_x"),
-                                   (ENGINE_NAMES[e] for e in ctx.engines()))),
+           "fft_engines": dict(zip(("x", "y", "deriv4_x", "roundtrip_x", "roundtrip_y"),
+                                   (ENGINE_NAMES[e] for e in ctx.engines()[:5])))
+                          | {"tensor_x": ("fused" if ctx.engines()[5] else "separate")},
            "fft_autotune": ctx.autotune_report}
     return ctx, res
 

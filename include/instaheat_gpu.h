@@ -172,15 +172,18 @@ int ih_variance_host(ih_context *c, double mean, const double *f_host, size_t n,
 
 /* ---- FFT autotuner (no reference counterpart; FFTW's planner flag
  * FFTW_DEFAULT_FLAG, parameters.sh, plays this role there) ----
- * Times every engine variant of the x and y passes and of the fused inverse
- * x pass of the RHS on the context's scratch spectra and keeps the fastest
- * per pass.  Until it is called the passes use the shared-memory Stockham
+ * Times every engine variant of the x and y passes, of the fused inverse x
+ * pass, of the x and y derivative round trips and of the last tensor x pass
+ * of the RHS on the context's scratch spectra and keeps the fastest per
+ * pass.  Until it is called the passes use the shared-memory Stockham
  * engine.  Results are identical across variants up to rounding.  The report
  * lists the timings and the choice (valid until the next ih_autotune). */
 int ih_autotune(ih_context *c);
 const char *ih_autotune_report(const ih_context *c);
 /* Pin or read the engine of one pass: pass 0 = x, 1 = y, 2 = the fused
- * inverse x pass; engine IH_FFT_STOCKHAM, IH_FFT_TWOSTEP (register two-step,
+ * inverse x pass, 3 / 4 = the x / y derivative round trips (two-step forms
+ * only), 5 = the last x pass of the tensor sources (0 = x passes then
+ * update_h, 1 = one kernel accumulating the TT projection); engine IH_FFT_STOCKHAM, IH_FFT_TWOSTEP (register two-step,
  * 128-byte tiles), IH_FFT_TWOSTEP_HALF (64-byte tiles), IH_FFT_PIPELINED
  * (register two-step in persistent CTAs that copy the next tile in with
  * cp.async while transforming the current one) or IH_FFT_THREESTEP (three
@@ -189,6 +192,12 @@ enum { IH_FFT_STOCKHAM = 0, IH_FFT_TWOSTEP = 1, IH_FFT_TWOSTEP_HALF = 2, IH_FFT_
        IH_FFT_THREESTEP = 4 };
 int ih_fft_set_engine(ih_context *c, int pass, int engine);
 int ih_fft_get_engine(const ih_context *c, int pass);
+/* How an RHS without the filter and output flags forms the derivatives of
+ * phi (on by default): 1 = round trips along x and y on the z spectrum of
+ * phi (the y and x transforms that cancel are not done), 0 = from the full
+ * 3-D spectrum as the filtered / output RHS does.  The two agree to
+ * rounding. */
+int ih_rhs_roundtrip(ih_context *c, int on);
 
 /* CUDA graphs (no reference counterpart): each DOPRI853 try (its 11 stage
  * combinations and RHS evaluations, the final combination and the error

@@ -20,7 +20,7 @@ int check_launch(Ctx *c, const char *what) {
 const char *kernel_kind_name(int k) {
   static const char *names[KK_COUNT] = {
       "k_fft_xy",       "k_fft_zr2c",    "k_fft_zc2r",       "k_fft_x_deriv4_inv",
-      "k_fft_z_rhs_fused", "k_update_h", "k_update_phi_psi", "k_filter_spectra",
+      "k_fft_xy_rt",    "k_fft_x_tensor", "k_fft_z_rhs_fused", "k_update_h", "k_update_phi_psi", "k_filter_spectra",
       "k_lincomb",      "k_dopri_final"};
   return (k >= 0 && k < KK_COUNT) ? names[k] : "unknown";
 }
@@ -485,13 +485,27 @@ const char *ih_autotune_report(const ih_context *h) {
 
 int ih_fft_set_engine(ih_context *h, int pass, int engine) {
   CTX_CHECK(h);
-  if (pass < 0 || pass > 2 || engine < 0 || engine >= FV_COUNT) return IH_ERR_ARG;
+  if (pass < 0 || pass > 5 || engine < 0 || engine >= FV_COUNT) return IH_ERR_ARG;
   if (pass == 2 && engine == FV_THREESTEP) return IH_ERR_ARG;
+  if ((pass == 3 || pass == 4) && engine != FV_TWOSTEP && engine != FV_TWOSTEP_HALF)
+    return IH_ERR_ARG;
+  if (pass == 5 && engine > 1) return IH_ERR_ARG;
   if (pass < 2) {
     h->c.xy_var[pass] = engine;
-  } else {
+  } else if (pass == 2) {
     h->c.d4_var = engine;
+  } else if (pass < 5) {
+    h->c.rt_var[pass - 3] = engine;
+  } else {
+    h->c.tensor_fused = engine;
   }
+  h->c.graph_epoch += 1;
+  return IH_OK;
+}
+
+int ih_rhs_roundtrip(ih_context *h, int on) {
+  CTX_CHECK(h);
+  h->c.roundtrip = on ? 1 : 0;
   h->c.graph_epoch += 1;
   return IH_OK;
 }
@@ -503,8 +517,10 @@ int ih_graphs_enable(ih_context *h, int on) {
 }
 
 int ih_fft_get_engine(const ih_context *h, int pass) {
-  if (!h || pass < 0 || pass > 2) return -1;
-  return pass < 2 ? h->c.xy_var[pass] : h->c.d4_var;
+  if (!h || pass < 0 || pass > 5) return -1;
+  if (pass < 2) return h->c.xy_var[pass];
+  if (pass == 5) return h->c.tensor_fused;
+  return pass == 2 ? h->c.d4_var : h->c.rt_var[pass - 3];
 }
 
 int ih_fft_host(ih_context *h, const double *in, double *out_c) {
@@ -855,6 +871,9 @@ int ih_ensemble_autotune(ih_ensemble *e) {
       c->xy_var[0] = twin->xy_var[0];
       c->xy_var[1] = twin->xy_var[1];
       c->d4_var = twin->d4_var;
+      c->rt_var[0] = twin->rt_var[0];
+      c->rt_var[1] = twin->rt_var[1];
+      c->tensor_fused = twin->tensor_fused;
       c->tune_report = twin->tune_report;
       c->graph_epoch += 1;
     } else {

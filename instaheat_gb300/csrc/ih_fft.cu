@@ -34,6 +34,7 @@
 #include <utility>
 #include <unordered_map>
 #include "ih_internal.cuh"
+#include "ih_tensor.cuh"
 
 namespace ih {
 
@@ -89,6 +90,19 @@ __host__ __device__ constexpr int round_warp(int n) { return n < 32 ? 32 : (n + 
 // register column of the wider step
 template <int L, int B> __host__ __device__ constexpr int pass_threads() {
   return round_warp(max_r<L>() * B);
+}
+// Row of the exchange buffer [L][B] of the two-step kernels (no padding).
+// A warp's access touches one row per thread group q (rows q R2 + k2 when
+// step 1 writes, q R1 + n1 when step 2 writes, consecutive rows when the
+// next step reads).  With half-line rows (64 bytes) rows of equal parity
+// share a half of the banks, and R1, R2 >= 8 make the written rows of one
+// warp all even or all odd: the row is swapped with its neighbour (r ^ 1) on
+// alternate blocks of R1 (and R2) rows, which puts the groups of every such
+// access on both halves, a permutation of the rows.
+template <int L> __device__ __forceinline__ int xrow(int r) {
+  constexpr int a = clog2(Fac<L>::R1), b = clog2(Fac<L>::R2);
+  const int f = (a == b) ? (r >> a) : ((r >> a) ^ (r >> b));
+  return r ^ (f & 1);
 }
 // exp(-2 pi i m/16) for a compile-time m: the cosines and sines of multiples
 // of pi/8 (cos pi/8, sin pi/8, sqrt(1/2)), correctly rounded in double
@@ -318,7 +332,7 @@ template <typename T, int L, int B>
 __global__ void __launch_bounds__(pass_threads<L, B>()) k_fft_xy_2s(C2<T> *data, long long astride, long long sj, long long so, int mz,
                          int sign, const C2<T> *twg) {
   constexpr int R1 = Fac<L>::R1, R2 = Fac<L>::R2;
-  constexpr int LB = clog2(B), P = B + 1;
+  constexpr int LB = clog2(B), P = B;
   extern __shared__ __align__(16) unsigned char smraw[];
   C2<T> *tw = reinterpret_cast<C2<T> *>(smraw);
   C2<T> *x1 = tw + L;  // [n1*R2 + k2][P]
@@ -337,14 +351,14 @@ __global__ void __launch_bounds__(pass_threads<L, B>()) k_fft_xy_2s(C2<T> *data,
     reg_dft<T, R2>(v, tw, L / R2, sign);
 #pragma unroll
     for (int k2 = 0; k2 < R2; ++k2)
-      x1[(n1 * R2 + k2) * P + b] = (k2 == 0) ? v[k2] : cmul(v[k2], twid(tw, (n1 * k2) & (L - 1), sign));
+      x1[xrow<L>(n1 * R2 + k2) * P + b] = (k2 == 0) ? v[k2] : cmul(v[k2], twid(tw, (n1 * k2) & (L - 1), sign));
   }
   __syncthreads();
   if (tid < R2 * B) {
     const int b = tid & (B - 1), k2 = tid >> LB;
     C2<T> u[R1];
 #pragma unroll
-    for (int n1 = 0; n1 < R1; ++n1) u[n1] = x1[(n1 * R2 + k2) * P + b];
+    for (int n1 = 0; n1 < R1; ++n1) u[n1] = x1[xrow<L>(n1 * R2 + k2) * P + b];
     reg_dft<T, R1>(u, tw, L / R1, sign);
     if (b < bv) {
 #pragma unroll
@@ -684,15 +698,21 @@ __device__ __forceinline__ void zc2r_twiddles(const C2<T> *__restrict__ twz, int
 }
 
 template <typename T, int H>
-__device__ __forceinline__ void zc2r_load(const C2<T> *row, int t, int gbase, bool valid,
-                                          const C2<T> (&wnat)[ZGeo<H>::R],
+__device__ __forceinline__ void zc2r_fetch(const C2<T> *row, int t, bool valid,
+                                           C2<T> (&x)[ZGeo<H>::R], C2<T> &xH) {
+  using Gm = ZGeo<H>;
+#pragma unroll
+  for (int n = 0; n < Gm::R; ++n) x[n] = valid ? row[t + Gm::W * n] : mk2<T>(0, 0);
+  xH = (valid && t == 0) ? row[H] : mk2<T>(0, 0);
+}
+// the c2r pre-processing of a fetched row (element k = t + W n in register
+// n of lane t, element H in xH of lane 0)
+template <typename T, int H>
+__device__ __forceinline__ void zc2r_prep(const C2<T> (&x)[ZGeo<H>::R], C2<T> xH, int t,
+                                          int gbase, const C2<T> (&wnat)[ZGeo<H>::R],
                                           C2<T> (&z)[ZGeo<H>::R]) {
   using Gm = ZGeo<H>;
   constexpr int R = Gm::R, W = Gm::W;
-  C2<T> x[R];
-#pragma unroll
-  for (int n = 0; n < R; ++n) x[n] = valid ? row[t + W * n] : mk2<T>(0, 0);
-  const C2<T> xH = (valid && t == 0) ? row[H] : mk2<T>(0, 0);
   const int src = gbase + ((W - t) & (W - 1));
 #pragma unroll
   for (int n = 0; n < R; ++n) {
@@ -703,6 +723,14 @@ __device__ __forceinline__ void zc2r_load(const C2<T> *row, int t, int gbase, bo
     const C2<T> o = cmul(d, wnat[n]);
     z[n] = mk2<T>(e.x - o.y, e.y + o.x);  // E + i O
   }
+}
+template <typename T, int H>
+__device__ __forceinline__ void zc2r_load(const C2<T> *row, int t, int gbase, bool valid,
+                                          const C2<T> (&wnat)[ZGeo<H>::R],
+                                          C2<T> (&z)[ZGeo<H>::R]) {
+  C2<T> x[ZGeo<H>::R], xH;
+  zc2r_fetch<T, H>(row, t, valid, x, xH);
+  zc2r_prep<T, H>(x, xH, t, gbase, wnat, z);
 }
 
 // a row held scrambled (register k1 of lane t = element k1 + R brev(t))
@@ -905,7 +933,7 @@ template <typename T, int L, int B>
 __global__ void __launch_bounds__(pass_threads<L, B>(), (d4_min_blocks<T, L, B>())) k_fft_x_deriv4_2s(const C2<T> *phihat, C2<T> *out, long long ostride, Geom g,
                                    const C2<T> *twg) {
   constexpr int R1 = Fac<L>::R1, R2 = Fac<L>::R2;
-  constexpr int LB = clog2(B), P = B + 1;
+  constexpr int LB = clog2(B), P = B;
   extern __shared__ __align__(16) unsigned char smraw[];
   C2<T> *tw = reinterpret_cast<C2<T> *>(smraw);
   C2<T> *x1 = tw + L;
@@ -956,14 +984,14 @@ __global__ void __launch_bounds__(pass_threads<L, B>(), (d4_min_blocks<T, L, B>(
       reg_dft<T, R2>(v, tw, L / R2, +1);
 #pragma unroll
       for (int k2 = 0; k2 < R2; ++k2)
-        x1[(n1 * R2 + k2) * P + b1] = (k2 == 0) ? v[k2] : cmul(v[k2], twid(tw, (n1 * k2) & (L - 1), +1));
+        x1[xrow<L>(n1 * R2 + k2) * P + b1] = (k2 == 0) ? v[k2] : cmul(v[k2], twid(tw, (n1 * k2) & (L - 1), +1));
     }
     __syncthreads();
     if (tid < R2 * B) {
       const int b = tid & (B - 1), k2 = tid >> LB;
       C2<T> u[R1];
 #pragma unroll
-      for (int m1 = 0; m1 < R1; ++m1) u[m1] = x1[(m1 * R2 + k2) * P + b];
+      for (int m1 = 0; m1 < R1; ++m1) u[m1] = x1[xrow<L>(m1 * R2 + k2) * P + b];
       reg_dft<T, R1>(u, tw, L / R1, +1);
       C2<T> *o = out + a * ostride + off;
       if (b < bv) {
@@ -1069,6 +1097,254 @@ __global__ void __launch_bounds__(pass_threads<L, B>(), 2) k_fft_x_deriv4_pipe(c
   cp_async_wait<0>();
 }
 
+// ---------------------------------------------------------------------------
+// Round trip along x or y on the z spectra Z[x][y][kz] of phi.  Derivatives
+// along one axis commute with the transforms along the others, so
+//   out0 = scale * IFFT(i k   FFT(in))     (first derivative, 0 on Nyquist)
+//   out1 = scale * IFFT(-k^2 FFT(in))      (second derivative)
+// along the pencil axis give d/dx Z, d2/dx2 Z (or the y ones) without the y
+// (or x) transforms; k = ku * (index folded to [-L/2, L/2)), k^2 = k2u * |index|^2
+// as setup.c:609-666 defines the k vectors.
+// Forward two-step: step 1 (thread b, n1) DFT_R2 over x[n1 + R1 n2] and the
+// twiddle w^(-n1 k2); exchange; step 2 (thread b, k2) DFT_R1 over n1 ->
+// X[k2 + R2 k1] in registers.  The inverse starts from that layout: DFT_R1
+// over k1, twiddle w^(n1 k2), exchange, DFT_R2 over k2 -> x[n1 + R1 n2], the
+// step-1 thread layout again.  Two exchange buffers, one per output.
+template <typename T, int L, int B>
+__global__ void __launch_bounds__(pass_threads<L, B>()) k_fft_xy_rt(
+    const C2<T> *in, C2<T> *out0, C2<T> *out1, long long sj, long long so, int mz, double ku,
+    double k2u, double scale, const C2<T> *twg) {
+  constexpr int R1 = Fac<L>::R1, R2 = Fac<L>::R2;
+  constexpr int LB = clog2(B), P = B;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<T> *tw = reinterpret_cast<C2<T> *>(smraw);
+  C2<T> *e0 = tw + L;      // [L][P]
+  C2<T> *e1 = e0 + L * P;  // [L][P]
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int z0 = blockIdx.x * B;
+  const int bv = min(B, mz - z0);
+  const long long off = (long long)blockIdx.y * so + z0;
+  load_table(tw, twg, L, tid, nt);
+  __syncthreads();
+  const int b = tid & (B - 1), q = tid >> LB;
+  if (q < R1) {  // q = n1
+    C2<T> v[R2];
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2)
+      v[n2] = (b < bv) ? in[off + (long long)(q + R1 * n2) * sj + b] : mk2<T>(0, 0);
+    reg_dft<T, R2>(v, tw, L / R2, -1);
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2)
+      e0[xrow<L>(q * R2 + k2) * P + b] = (k2 == 0) ? v[k2] : cmul(v[k2], twid(tw, (q * k2) & (L - 1), -1));
+  }
+  __syncthreads();
+  C2<T> u[R1];
+  if (q < R2) {  // q = k2
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) u[n1] = e0[xrow<L>(n1 * R2 + q) * P + b];
+  }
+  __syncthreads();  // e0 is rewritten below
+  if (q < R2) {
+    reg_dft<T, R1>(u, tw, L / R1, -1);
+    const T sc = (T)scale;
+#pragma unroll
+    for (int o = 0; o < 2; ++o) {
+      C2<T> w[R1];
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) {
+        const int k = q + R2 * k1;
+        if (o == 0) {
+          const T f = (2 * k == L) ? (T)0 : kfac<T>(ku, (k > L / 2) ? (k - L) : k) * sc;
+          w[k1] = mk2<T>(-u[k1].y * f, u[k1].x * f);  // X * i k
+        } else {
+          const int ka = (k > L / 2) ? (L - k) : k;
+          const T f = -((T)k2u * (T)ka * (T)ka) * sc;
+          w[k1] = mk2<T>(u[k1].x * f, u[k1].y * f);  // -X k^2
+        }
+      }
+      reg_dft<T, R1>(w, tw, L / R1, +1);
+      C2<T> *e = o ? e1 : e0;
+#pragma unroll
+      for (int n1 = 0; n1 < R1; ++n1)
+        e[xrow<L>(q * R1 + n1) * P + b] = (n1 == 0) ? w[n1] : cmul(w[n1], twid(tw, (n1 * q) & (L - 1), +1));
+    }
+  }
+  __syncthreads();
+  if (q < R1) {  // q = n1
+#pragma unroll
+    for (int o = 0; o < 2; ++o) {
+      const C2<T> *e = o ? e1 : e0;
+      C2<T> v[R2];
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2) v[k2] = e[xrow<L>(k2 * R1 + q) * P + b];
+      reg_dft<T, R2>(v, tw, L / R2, +1);
+      C2<T> *dst = (o ? out1 : out0) + off;
+      if (b < bv) {
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2) {
+          dst[(long long)(q + R1 * n2) * sj + b] = v[n2];
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Last forward pass of the tensor sources fused with update_h.  The x
+// transforms of the six S_ij half spectra (after their z and y passes) of a
+// tile of B pencils (one y, B consecutive kz: rows of 32 bytes) end in
+// registers and go straight to the per-mode TT projection and tensor
+// equation of motion (toolbox.c:311-346, 363-397): the six x-transformed
+// spectra are neither written nor read back.
+// Radix-4 Stockham (a radix-2 first stage when log2 L is odd), L/4 threads
+// per pencil: thread j reads x[j + r L/4] (r = 0..3) from global memory,
+// exchanges through shared memory between stages and ends holding
+// X[j + r L/4].  A radix-4 stage of span Ns (the product of the earlier
+// radices) takes data[j + r L/4] times w_L^(r (j mod Ns) L / (4 Ns)), a 4-point
+// DFT, and puts the outputs at data[(j / Ns) 4 Ns + j mod Ns + r Ns].
+// Buffer rows (32 bytes) are swizzled, x ^ ((x >> 2) & 3), so that every
+// stage's accesses of a warp (8 threads j x B pencils) spread over the four
+// 32-byte bank groups.
+__device__ __forceinline__ int srow4(int x) { return x ^ ((x >> 2) & 3); }
+
+template <typename T>
+__device__ __forceinline__ void dft4_fwd(C2<T> (&v)[4]) {
+  const C2<T> s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+  const C2<T> s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+  const C2<T> j13 = mk2<T>(d13.y, -d13.x);  // -i (x1 - x3)
+  v[0] = cadd(s02, s13);
+  v[2] = csub(s02, s13);
+  v[1] = cadd(d02, j13);
+  v[3] = csub(d02, j13);
+}
+
+template <typename T> __host__ __device__ constexpr int tensor_tile() {
+  return 32 / (int)(2 * sizeof(T));  // pencils of a 32-byte row
+}
+
+// resident CTAs asked of the register allocator: 24 warps per SM (FP32)
+template <typename T, int L, int B> __host__ __device__ constexpr int xt_min_blocks() {
+  return (sizeof(T) == 4 && 768 / (L / 4 * B) > 1) ? 768 / (L / 4 * B) : 1;
+}
+// shared memory of k_fft_x_tensor: twiddles and two exchange buffers [L][B]
+template <typename T> constexpr size_t xt_smem(int L, int B) {
+  return sizeof(C2<T>) * ((size_t)L + 2 * (size_t)L * B);
+}
+
+template <typename T, int L, int B>
+__global__ void __launch_bounds__(L / 4 * B, (xt_min_blocks<T, L, B>())) k_fft_x_tensor(
+    const C2<T> *s03, const C2<T> *s45, long long astride, const T *__restrict__ y,
+    T *__restrict__ out, const RhsScalars *rs, Geom g, const C2<T> *twg) {
+  constexpr int Q = L / 4, LB = clog2(B);
+  constexpr bool R2F = (clog2(L) & 1) != 0;
+  constexpr int NS0 = R2F ? 2 : 4;                                   // span after the first stage
+  constexpr int NST = L == 4 ? 0 : (clog2(Q) - clog2(NS0)) / 2 + 1;  // radix-4 stages left
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<T> *tw = reinterpret_cast<C2<T> *>(smraw);
+  C2<T> *buf = tw + L;  // two [L][B] exchange buffers
+  const int tid = threadIdx.x;
+  load_table(tw, twg, L, tid, Q * B);
+  const int b = tid & (B - 1), j = tid >> LB;
+  const int mz = g.mz, z0 = blockIdx.x * B, bv = min(B, mz - z0);
+  const int yj = blockIdx.y;
+  const long long sj = (long long)g.ny * mz;
+  const long long off = (long long)yj * mz + z0;
+  auto src_of = [&](int a) {
+    return (a < 4 ? s03 + a * astride : s45 + (a - 4) * astride) + off;
+  };
+  C2<T> nxt[4];  // the next spectrum's inputs, loaded while this one is transformed
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+    nxt[r] = (b < bv) ? src_of(0)[(long long)(j + r * Q) * sj + b] : mk2<T>(0, 0);
+  // the thread's four modes (i = j + r L/4, yj, z0 + b): k components; the
+  // projected sources accumulate spectrum by spectrum (tensor_coef)
+  Mode m;
+  m.j = yj;
+  m.k = z0 + b;
+  const int branch = (m.k != 0) ? 0 : (m.j != 0 ? 1 : 2);
+  T kx[4], inv[4], ky = 0, kz = 0;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    m.i = j + r * Q;
+    const ModeK<T> q = mode_k<T>(g, m);
+    kx[r] = q.kx;
+    ky = q.ky;
+    kz = q.kz;
+    inv[r] = q.ksq > (T)0 ? (T)1.0 / q.ksq : (T)0;
+  }
+  C2<T> n0[4], n1[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) n0[r] = n1[r] = mk2<T>(0, 0);
+  int wb = 0;  // buffer of the next write
+  __syncthreads();
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    C2<T> v[4] = {nxt[0], nxt[1], nxt[2], nxt[3]};
+    if (a + 1 < 6) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        nxt[r] = (b < bv) ? src_of(a + 1)[(long long)(j + r * Q) * sj + b] : mk2<T>(0, 0);
+    }
+    if constexpr (L == 4) {
+      dft4_fwd<T>(v);
+    } else {
+      C2<T> *d = buf + wb * L * B;
+      if constexpr (R2F) {  // radix 2 on (x, x + L/2) for x = j and x = j + L/4
+        d[srow4(2 * j) * B + b] = cadd(v[0], v[2]);
+        d[srow4(2 * j + 1) * B + b] = csub(v[0], v[2]);
+        d[srow4(2 * (j + Q)) * B + b] = cadd(v[1], v[3]);
+        d[srow4(2 * (j + Q) + 1) * B + b] = csub(v[1], v[3]);
+      } else {
+        dft4_fwd<T>(v);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) d[srow4(4 * j + r) * B + b] = v[r];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int st = 0; st < NST; ++st) {
+        const int Ns = NS0 << (2 * st);
+        const C2<T> *s = buf + wb * L * B;
+        const int jm = j & (Ns - 1);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          v[r] = s[srow4(j + r * Q) * B + b];
+          if (r > 0) v[r] = cmul(v[r], tw[r * jm * (L / (4 * Ns))]);
+        }
+        dft4_fwd<T>(v);
+        if (st + 1 < NST) {
+          wb ^= 1;
+          C2<T> *d2 = buf + wb * L * B;
+          const int base = (j / Ns) * 4 * Ns + jm;
+#pragma unroll
+          for (int r = 0; r < 4; ++r) d2[srow4(base + r * Ns) * B + b] = v[r];
+          __syncthreads();
+        }
+      }
+      wb ^= 1;  // the next spectrum writes the buffer not being read now
+    }
+    // v[r] = X_a[j + r L/4]
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      T al, be;
+      tensor_coef<T>(a, branch, kx[r], ky, kz, kx[r] * inv[r], ky * inv[r], kz * inv[r], al, be);
+      n0[r] = mk2<T>(n0[r].x + al * v[r].x, n0[r].y + al * v[r].y);
+      n1[r] = mk2<T>(n1[r].x + be * v[r].x, n1[r].y + be * v[r].y);
+    }
+  }
+  if (b < bv) {
+    const TensorConsts<T> tc(rs);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      m.i = j + r * Q;
+      const long long id = (long long)m.i * sj + off + b;
+      const T ksq = mode_k<T>(g, m).ksq;
+      const C2<T> zero = mk2<T>(0, 0);
+      tensor_eom<T>(g, id, id != 0 ? n0[r] : zero, id != 0 ? n1[r] : zero, id != 0 ? ksq : (T)0,
+                    tc, y, out);
+    }
+  }
+}
+
 // energy density and pressure at one point (see above)
 template <typename T, bool MIXED>
 __device__ __forceinline__ void rho_p(T dx, T dy, T dz, T phi, T dph, T ps, T inv_a2, T m2, T third,
@@ -1092,8 +1368,12 @@ __device__ __forceinline__ void rho_p(T dx, T dy, T dz, T phi, T dph, T ps, T in
   }
 }
 
-template <typename T, bool MIXED, int H>
-__global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_z_rhs_fused(const C2<T> *d4, long long dstride, const T *yfl,
+// ZSRC: the inputs are the round-trip outputs d/dx Z, d/dy Z (arrays 0, 1),
+// the y and x parts of the laplacian (arrays 2, 3) and Z itself (array 4); the
+// z derivative and the z part of the laplacian are applied to Z here.
+// Otherwise arrays 0..3 hold the four full derivative spectra.
+template <typename T, bool MIXED, int H, bool ZSRC>
+__global__ void __launch_bounds__(32 * zwarps<T>(), (sizeof(T) == 4 && H <= 128 ? 3 : 1)) k_fft_z_rhs_fused(const C2<T> *d4, long long dstride, const T *yfl,
                                   const double *ysc, T *lap, T *pout, T *rhoout, C2<T> *s6,
                                   long long sstride4, C2<T> *s6b, int gw, double *partials,
                                   Geom g, const C2<T> *__restrict__ twh, const C2<T> *__restrict__ twz) {
@@ -1114,9 +1394,41 @@ __global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_z_rhs_fused(const C2<T
   {
     C2<T> wnat[R];
     zc2r_twiddles<T, H>(twz, t, wnat);
+    const T invnz = (T)(1.0 / (double)g.nz);
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-      zc2r_load<T, H>(d4 + a * dstride + row * (H + 1), t, lane & ~(W - 1), valid, wnat, d[a]);
+      C2<T> x[R], xH;
+      if constexpr (ZSRC) {
+        // Z is fetched for a = 2 and again (from L1) for a = 3 rather than
+        // kept live across a transform
+        C2<T> zx[R], zH;
+        if (a >= 2) zc2r_fetch<T, H>(d4 + 4 * dstride + row * (H + 1), t, valid, zx, zH);
+        if (a == 2) {  // i kz Z / nz, zero on the Nyquist index
+#pragma unroll
+          for (int n = 0; n < R; ++n) {
+            const T f = kfac<T>(g.kzu, t + W * n) * invnz;
+            x[n] = mk2<T>(-zx[n].y * f, zx[n].x * f);
+          }
+          xH = mk2<T>(0, 0);
+        } else {
+          zc2r_fetch<T, H>(d4 + a * dstride + row * (H + 1), t, valid, x, xH);
+          if (a == 3) {  // x part (array 3) + y part (array 2) + (-kz^2) Z / nz
+            C2<T> yx[R], yH;
+            zc2r_fetch<T, H>(d4 + 2 * dstride + row * (H + 1), t, valid, yx, yH);
+#pragma unroll
+            for (int n = 0; n < R; ++n) {
+              const int kz = t + W * n;
+              const T f = -((T)g.kz2 * (T)kz * (T)kz) * invnz;
+              x[n] = mk2<T>(x[n].x + yx[n].x + f * zx[n].x, x[n].y + yx[n].y + f * zx[n].y);
+            }
+            const T fH = -((T)g.kz2 * (T)H * (T)H) * invnz;
+            xH = mk2<T>(xH.x + yH.x + fH * zH.x, xH.y + yH.y + fH * zH.y);
+          }
+        }
+      } else {
+        zc2r_fetch<T, H>(d4 + a * dstride + row * (H + 1), t, valid, x, xH);
+      }
+      zc2r_prep<T, H>(x, xH, t, lane & ~(W - 1), wnat, d[a]);
       zfft_dif<+1, T, H>(d[a], w, twh);
       zunscramble<T, H>(d[a], t, srow);
     }
@@ -1274,7 +1586,7 @@ struct XYLaunch {
   }
   template <int L, int B>
   int run_2s(dim3 grid, long long sj, long long so, const C2<T> *tw) {
-    const size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * (B + 1));
+    const size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * B);
     cudaFuncSetAttribute(k_fft_xy_2s<T, L, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_fft_xy_2s<T, L, B><<<grid, pass_threads<L, B>(), sm, c->stream>>>(data, stride, sj, so,
                                                                          c->g.mz, sign, tw);
@@ -1429,7 +1741,7 @@ struct D4Launch {
   int run_2s() {
     const Geom &g = c->g;
     dim3 grid((g.mz + B - 1) / B, g.ny, 1);
-    const size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * (B + 1));
+    const size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * B);
     cudaFuncSetAttribute(k_fft_x_deriv4_2s<T, L, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sm);
     k_fft_x_deriv4_2s<T, L, B><<<grid, pass_threads<L, B>(), sm, c->stream>>>(
@@ -1489,6 +1801,86 @@ int fft_x_deriv4_inv(Ctx *c, const C2<T> *phihat, C2<T> *out, long long out_stri
 }
 
 template <typename T>
+struct RTLaunch {
+  Ctx *c;
+  const C2<T> *z;
+  C2<T> *d1, *d2;
+  int axis, var;
+  template <int L, int B>
+  int go(dim3 grid, long long sj, long long so, double ku, double k2u, double scale,
+         const C2<T> *tw) {
+    const size_t sm = sizeof(C2<T>) * ((size_t)L + 2 * (size_t)L * B);
+    cudaFuncSetAttribute(k_fft_xy_rt<T, L, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm);
+    k_fft_xy_rt<T, L, B><<<grid, pass_threads<L, B>(), sm, c->stream>>>(
+        z, d1, d2, sj, so, c->g.mz, ku, k2u, scale, tw);
+    return IH_OK;
+  }
+  template <int L>
+  int run() {
+    if constexpr (L == 512 && !allow512<T>()) {
+      return IH_ERR_ARG;
+    } else {
+      constexpr int B = tileB<T>();
+      const Geom &g = c->g;
+      const long long sj = axis == 0 ? (long long)g.ny * g.mz : g.mz;
+      const long long so = axis == 0 ? g.mz : (long long)g.ny * g.mz;
+      const int outer = axis == 0 ? g.ny : g.nx;
+      const double ku = axis == 0 ? g.kxu : g.kyu;
+      const double k2u = axis == 0 ? g.kx2 : g.ky2;
+      const double scale = 1.0 / ((double)L * (double)g.nz);
+      const C2<T> *tw = tab<T>(axis == 0 ? c->tw_x : c->tw_y);
+      if (var == FV_TWOSTEP)
+        return go<L, B>(dim3((g.mz + B - 1) / B, outer, 1), sj, so, ku, k2u, scale, tw);
+      constexpr int Bh = B / 2;
+      return go<L, Bh>(dim3((g.mz + Bh - 1) / Bh, outer, 1), sj, so, ku, k2u, scale, tw);
+    }
+  }
+};
+
+template <typename T>
+struct XTLaunch {
+  Ctx *c;
+  const C2<T> *s03, *s45;
+  const T *y;
+  T *out;
+  template <int L>
+  int run() {
+    if constexpr (L == 512 && !allow512<T>()) {
+      return IH_ERR_ARG;
+    } else {
+      constexpr int B = tensor_tile<T>();
+      const Geom &g = c->g;
+      const size_t sm = xt_smem<T>(L, B);
+      cudaFuncSetAttribute(k_fft_x_tensor<T, L, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sm);
+      k_fft_x_tensor<T, L, B><<<dim3((g.mz + B - 1) / B, g.ny, 1), L / 4 * B, sm, c->stream>>>(
+          s03, s45, g.M, y, out, c->rs, g, tab<T>(c->tw_x));
+      return IH_OK;
+    }
+  }
+};
+
+template <typename T>
+int fft_x_tensor(Ctx *c, const C2<T> *s03, const C2<T> *s45, const T *y, T *out) {
+  const Geom &g = c->g;
+  prof_begin(c, KK_X_TENSOR);
+  IH_TRY(dispatch_len(g.nx, XTLaunch<T>{c, s03, s45, y, out}, allow512<T>()));
+  prof_end(c, KK_X_TENSOR, 6.0 * g.M * sizeof(C2<T>) + 8.0 * g.Next * sizeof(T));
+  return check_launch(c, "k_fft_x_tensor");
+}
+
+template <typename T>
+int fft_xy_roundtrip(Ctx *c, const C2<T> *z, C2<T> *d1, C2<T> *d2, int axis) {
+  const Geom &g = c->g;
+  prof_begin(c, KK_XY_RT);
+  IH_TRY(dispatch_len(axis == 0 ? g.nx : g.ny, RTLaunch<T>{c, z, d1, d2, axis, c->rt_var[axis]},
+                      allow512<T>()));
+  prof_end(c, KK_XY_RT, 3.0 * g.M * sizeof(C2<T>));
+  return check_launch(c, "k_fft_xy_rt");
+}
+
+template <typename T>
 struct FusedLaunch {
   Ctx *c;
   const C2<T> *d4;
@@ -1499,6 +1891,19 @@ struct FusedLaunch {
   int gw;
   double *partials;
   int *nblk_out;
+  int zsrc;
+  template <int H, bool ZSRC>
+  void launch(unsigned nblk, int nt, long long M, C2<T> *s6b) {
+    if constexpr (sizeof(T) == 4) {
+      k_fft_z_rhs_fused<T, true, H, ZSRC><<<nblk, nt, 0, c->stream>>>(
+          d4, M, yfl, ysc, lap, p, rho, s6, M, s6b, gw, partials, c->g, tab<T>(c->tw_h),
+          tab<T>(c->tw_z));
+    } else {
+      k_fft_z_rhs_fused<T, false, H, ZSRC><<<nblk, nt, 0, c->stream>>>(
+          d4, M, yfl, ysc, lap, p, rho, s6, M, s6b, gw, partials, c->g, tab<T>(c->tw_h),
+          tab<T>(c->tw_z));
+    }
+  }
   template <int H>
   int run() {
     if constexpr (H > 256) {
@@ -1515,18 +1920,10 @@ struct FusedLaunch {
       const int nt = 32 * zwarps<T>();
       const long long M = g.M;
       C2<T> *s6b = s6 + 5 * M;  // products 4 and 5 go to spec[5], spec[6]
-      if (c->mixed) {
-        if constexpr (sizeof(T) == 4) {
-          k_fft_z_rhs_fused<T, true, H><<<nblk, nt, 0, c->stream>>>(
-              d4, M, yfl, ysc, lap, p, rho, s6, M, s6b, gw, partials, g, tab<T>(c->tw_h),
-              tab<T>(c->tw_z));
-        }
+      if (zsrc) {
+        launch<H, true>(nblk, nt, M, s6b);
       } else {
-        if constexpr (sizeof(T) == 8) {
-          k_fft_z_rhs_fused<T, false, H><<<nblk, nt, 0, c->stream>>>(
-              d4, M, yfl, ysc, lap, p, rho, s6, M, s6b, gw, partials, g, tab<T>(c->tw_h),
-              tab<T>(c->tw_z));
-        }
+        launch<H, false>(nblk, nt, M, s6b);
       }
       *nblk_out = (int)nblk;
       return IH_OK;
@@ -1536,13 +1933,14 @@ struct FusedLaunch {
 
 template <typename T>
 int fft_z_rhs_fused(Ctx *c, const C2<T> *d4, const T *yfl, const double *ysc, T *lap, T *p,
-                    T *rho, C2<T> *s6, int gw, double *partials, int *nblocks_out) {
+                    T *rho, C2<T> *s6, int gw, double *partials, int *nblocks_out, int zsrc) {
   const Geom &g = c->g;
   prof_begin(c, KK_Z_RHS_FUSED);
-  IH_TRY(dispatch_len(g.h, FusedLaunch<T>{c, d4, yfl, ysc, lap, p, rho, s6, gw, partials, nblocks_out},
-                      false));
+  IH_TRY(dispatch_len(
+      g.h, FusedLaunch<T>{c, d4, yfl, ysc, lap, p, rho, s6, gw, partials, nblocks_out, zsrc},
+      false));
   prof_end(c, KK_Z_RHS_FUSED,
-           (double)(4 + (gw ? 6 : 0)) * g.M * sizeof(C2<T>) +
+           (double)(4 + (zsrc ? 1 : 0) + (gw ? 6 : 0)) * g.M * sizeof(C2<T>) +
                (double)(3 + 2 + (rho ? 1 : 0)) * g.N * sizeof(T));
   return check_launch(c, "k_fft_z_rhs_fused");
 }
@@ -1601,23 +1999,36 @@ static int autotune_t(Ctx *c) {
   const int prof = c->prof_on;
   c->prof_on = 0;
   const int reps = 3;
-  char line[160];
+  char line[256];
   std::string rep;
   int st = IH_OK;
-  for (int pass = 0; pass < 3 && st == IH_OK; ++pass) {  // x, y, fused x
-    int best = 0;
+  static const char *pass_name[5] = {"x", "y", "deriv4-x", "rt-x", "rt-y"};
+  int best_t = 0;
+  float tbest_t = 0.f;
+  // x, y, fused x, x and y round trips
+  for (int pass = 0; pass < 5 && st == IH_OK; ++pass) {
+    int best = -1;
     float tbest = 0.f;
     for (int v = 0; v < FV_COUNT && st == IH_OK; ++v) {
       if (pass == 2 && v == FV_THREESTEP) continue;  // the fused x pass has no three-step form
+      if (pass > 2 && v != FV_TWOSTEP && v != FV_TWOSTEP_HALF) continue;
       if (pass < 2) {
         c->xy_var[pass] = v;
-      } else {
+      } else if (pass == 2) {
         c->d4_var = v;
+      } else {
+        c->rt_var[pass - 3] = v;
       }
       float ms = 0.f;
       for (int r = 0; r <= reps && st == IH_OK; ++r) {  // r = 0: warm-up
         if (r == 1) cudaEventRecord(e0, c->stream);
-        st = pass < 2 ? fft_xy<T>(c, sp, M, 4, pass, -1) : fft_x_deriv4_inv<T>(c, sp + 4 * M, sp, M);
+        if (pass < 2)
+          st = fft_xy<T>(c, sp, M, 4, pass, -1);
+        else if (pass == 2)
+          st = fft_x_deriv4_inv<T>(c, sp + 4 * M, sp, M);
+        else
+          st = fft_xy_roundtrip<T>(c, sp + 4 * M, sp + (pass - 3) * M, sp + (6 - pass) * M,
+                                   pass - 3);  // the RHS's arrays: d/dx 0, d2/dx2 3, d/dy 1, d2/dy2 2
       }
       if (st != IH_OK) break;
       cudaEventRecord(e1, c->stream);
@@ -1627,26 +2038,55 @@ static int autotune_t(Ctx *c) {
         break;
       }
       ms /= reps;
-      snprintf(line, sizeof line, "%s %s %.1f us; ", pass == 0 ? "x" : (pass == 1 ? "y" : "deriv4-x"),
-               variant_name(v), 1e3 * ms);
+      snprintf(line, sizeof line, "%s %s %.1f us; ", pass_name[pass], variant_name(v), 1e3 * ms);
       rep += line;
-      if (v == 0 || ms < tbest) {
+      if (best < 0 || ms < tbest) {
         best = v;
         tbest = ms;
       }
     }
+    if (best < 0) break;
     if (pass < 2) {
       c->xy_var[pass] = best;
-    } else {
+    } else if (pass == 2) {
       c->d4_var = best;
+    } else {
+      c->rt_var[pass - 3] = best;
     }
   }
+  // the last x pass of the tensor sources: x passes + update_h, or fused
+  // (timed on the scratch spectra with the state vectors y -> ytmp)
+  for (int v = 0; v < 2 && st == IH_OK; ++v) {
+    c->tensor_fused = v;
+    float ms = 0.f;
+    for (int r = 0; r <= reps && st == IH_OK; ++r) {
+      if (r == 1) cudaEventRecord(e0, c->stream);
+      st = tensor_last_pass(c, sp, c->y.fl, c->ytmp.fl);
+    }
+    if (st != IH_OK) break;
+    cudaEventRecord(e1, c->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      c->err = "autotune: event timing failed";
+      st = IH_ERR_CUDA;
+      break;
+    }
+    ms /= reps;
+    snprintf(line, sizeof line, "tensor %s %.1f us; ", v ? "fused" : "separate", 1e3 * ms);
+    rep += line;
+    if (v == 0 || ms < tbest_t) {
+      best_t = v;
+      tbest_t = ms;
+    }
+  }
+  if (st == IH_OK) c->tensor_fused = best_t;
   c->prof_on = prof;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st != IH_OK) return st;
-  snprintf(line, sizeof line, "chosen: x %s, y %s, deriv4-x %s", variant_name(c->xy_var[0]),
-           variant_name(c->xy_var[1]), variant_name(c->d4_var));
+  snprintf(line, sizeof line, "chosen: x %s, y %s, deriv4-x %s, rt-x %s, rt-y %s, tensor %s",
+           variant_name(c->xy_var[0]), variant_name(c->xy_var[1]), variant_name(c->d4_var),
+           variant_name(c->rt_var[0]), variant_name(c->rt_var[1]),
+           c->tensor_fused ? "fused" : "separate");
   c->tune_report = rep + line;
   return IH_OK;
 }
@@ -1663,7 +2103,9 @@ int fft_autotune(Ctx *c) {
   template int fft_xy<T>(Ctx *, C2<T> *, long long, int, int, int);                             \
   template int fft_x_deriv4_inv<T>(Ctx *, const C2<T> *, C2<T> *, long long);                   \
   template int fft_z_rhs_fused<T>(Ctx *, const C2<T> *, const T *, const double *, T *, T *,    \
-                                  T *, C2<T> *, int, double *, int *);
+                                  T *, C2<T> *, int, double *, int *, int);                     \
+  template int fft_xy_roundtrip<T>(Ctx *, const C2<T> *, C2<T> *, C2<T> *, int);              \
+  template int fft_x_tensor<T>(Ctx *, const C2<T> *, const C2<T> *, const T *, T *);
 IH_INST(float)
 IH_INST(double)
 #undef IH_INST

@@ -78,6 +78,8 @@ enum KernelKind {
   KK_FFT_ZR2C,          // real-to-complex pass along z
   KK_FFT_ZC2R,          // complex-to-real pass along z
   KK_X_DERIV4,          // inverse x pass generating the 4 derivative spectra
+  KK_XY_RT,             // x or y round trip (derivative spectra of Z)
+  KK_X_TENSOR,          // last x pass of the S_ij spectra fused with update_h
   KK_Z_RHS_FUSED,       // last inverse z pass + pointwise + GW products
   KK_UPDATE_H,          // TT projection + tensor equation of motion
   KK_UPDATE_PHI_PSI,    // phi/psi equations of motion
@@ -93,6 +95,16 @@ struct Timer {                  // per-kind CUDA-event accumulation
   std::vector<cudaEvent_t> ev;  // pairs
   long launches = 0;
   double bytes = 0.0;           // algorithmic bytes of the timed launches
+};
+
+// FFT engine variants (fft_autotune picks one per pass)
+enum FftVariant {
+  FV_STOCKHAM = 0,      // shared-memory Stockham, tile of one 128-byte line of pencils
+  FV_TWOSTEP = 1,       // register two-step, tile of one 128-byte line
+  FV_TWOSTEP_HALF = 2,  // register two-step, tile of half a line
+  FV_PIPELINED = 3,     // register two-step, persistent CTAs, cp.async double buffering
+  FV_THREESTEP = 4,     // three register steps of <= 8 values (x/y passes only)
+  FV_COUNT
 };
 
 struct Ctx {
@@ -174,18 +186,12 @@ struct Ctx {
   // by fft_autotune; Stockham with 128-byte tiles until tuned
   int xy_var[2] = {0, 0};
   int d4_var = 0;
+  int rt_var[2] = {FV_TWOSTEP_HALF, FV_TWOSTEP_HALF};  // x, y round trips (two-step forms)
+  int roundtrip = 1;  // RHS without filter/output: round trips instead of full spectra
+  int tensor_fused = 0;  // update_h fused into the last x pass (autotuner's choice)
   std::string tune_report;
 };
 
-// FFT engine variants (fft_autotune picks one per pass)
-enum FftVariant {
-  FV_STOCKHAM = 0,      // shared-memory Stockham, tile of one 128-byte line of pencils
-  FV_TWOSTEP = 1,       // register two-step, tile of one 128-byte line
-  FV_TWOSTEP_HALF = 2,  // register two-step, tile of half a line
-  FV_PIPELINED = 3,     // register two-step, persistent CTAs, cp.async double buffering
-  FV_THREESTEP = 4,     // three register steps of <= 8 values (x/y passes only)
-  FV_COUNT
-};
 
 // ---------------------------------------------------------------------------
 // error helpers
@@ -237,14 +243,26 @@ int fft_xy(Ctx *c, C2<T> *data, long long stride, int count, int axis,
 template <typename T>
 int fft_x_deriv4_inv(Ctx *c, const C2<T> *phihat, C2<T> *out,
                      long long out_stride);
+// Round trips along x (axis 0) and y (axis 1) on the z spectra Z of phi:
+// d1 = IFFT(i k FFT(Z)) / (L nz), d2 = IFFT(-k^2 FFT(Z)) / (L nz), the
+// per-axis derivative spectra of the fused z pass.
+template <typename T>
+int fft_xy_roundtrip(Ctx *c, const C2<T> *z, C2<T> *d1, C2<T> *d2, int axis);
+// The forward x pass of the six S_ij spectra (arrays 0..3 at s03, 4..5 at
+// s45, stride M; z and y passes done) fused with update_h: writes the tensor
+// segments of out from those of y (toolbox.c:311-346, 363-397).
+template <typename T>
+int fft_x_tensor(Ctx *c, const C2<T> *s03, const C2<T> *s45, const T *y, T *out);
 // Fused last inverse z pass for the RHS: c2r of the four derivative spectra,
 // then per point (grad phi)^2, rho, p (and their FP64 block sums), writes the
 // laplacian and p (and rho), and when gw the six products d_i phi d_j phi
-// transformed forward along z into six half spectra.
+// transformed forward along z into six half spectra.  zsrc: the inputs are
+// the round-trip outputs (d/dx, d/dy, y and x laplacian parts, Z in the
+// arrays 0..4), and d/dz and the z part of the laplacian come from Z.
 template <typename T>
 int fft_z_rhs_fused(Ctx *c, const C2<T> *d4, const T *yfl, const double *ysc,
                     T *lap, T *p, T *rho, C2<T> *s6, int gw, double *partials,
-                    int *nblocks_out);
+                    int *nblocks_out, int zsrc);
 
 int fft_tables(Ctx *c);
 // time every engine variant of the x/y passes and the fused x pass on the
@@ -253,6 +271,8 @@ int fft_autotune(Ctx *c);
 
 // ---------------------------------------------------------------------------
 // RHS and helpers (ih_rhs.cu)
+// the last forward x pass of the six S_ij spectra + update_h (either form)
+int tensor_last_pass(Ctx *c, void *spec, const void *y, void *out);
 int rhs(Ctx *c, double t, Vec &y, Vec &k, int filter, int output,
         const Vec *smry_src);
 int reduce_mean(Ctx *c, const void *arr, long long n, double *dev_out);

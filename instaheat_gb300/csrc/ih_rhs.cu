@@ -16,16 +16,9 @@
 #include <float.h>
 #include <math.h>
 #include "ih_internal.cuh"
+#include "ih_tensor.cuh"
 
 namespace ih {
-
-template <typename T>
-__device__ __forceinline__ C2<T> mk2c(T x, T y) {
-  C2<T> r;
-  r.x = x;
-  r.y = y;
-  return r;
-}
 
 __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -77,37 +70,6 @@ __device__ double block_min(double v) {
   return r;
 }
 
-// mode index -> (i, j, k) of the half spectrum
-struct Mode {
-  int i, j, k;
-};
-__device__ __forceinline__ Mode mode_of(long long id, const Geom &g) {
-  Mode m;
-  m.k = (int)(id % g.mz);
-  long long r = id / g.mz;
-  m.j = (int)(r % g.ny);
-  m.i = (int)(r / g.ny);
-  return m;
-}
-// FP64 k components with the reference's Nyquist conventions
-__device__ __forceinline__ double kxf_of(const Geom &g, int i) {
-  return g.kxu * ((i > g.nx / 2) ? (i - g.nx) : i);
-}
-__device__ __forceinline__ double kyf_of(const Geom &g, int j) {
-  return g.kyu * ((j > g.ny / 2) ? (j - g.ny) : j);
-}
-__device__ __forceinline__ double kzf_of(const Geom &g, int k) { return g.kzu * k; }
-__device__ __forceinline__ double kz_deriv(const Geom &g, int k) {
-  return (2 * k == g.nz) ? 0.0 : g.kzu * k;
-}
-__device__ __forceinline__ double ksq64(const Geom &g, int i, int j, int k) {
-  double q = g.kz2 * k * k;
-  int ia = (i > g.nx / 2) ? (g.nx - i) : i;
-  int ja = (j > g.ny / 2) ? (g.ny - j) : j;
-  q += g.kx2 * ia * ia;
-  q += g.ky2 * ja * ja;
-  return q;
-}
 
 // ---------------------------------------------------------------------------
 // filter mask (setup.c:710-754), kept in T
@@ -256,14 +218,10 @@ __global__ void k_update_phi_psi(const T *__restrict__ y, const double *ysc,
 // update_h with the TT projection (toolbox.c:311-346, 363-397).  s holds the
 // six S_ij spectra, spectra 4 and 5 at s + 5M.
 template <typename T>
-__global__ void k_update_h(const C2<T> *__restrict__ s, const T *__restrict__ y,
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 5 : 2)) k_update_h(const C2<T> *__restrict__ s, const T *__restrict__ y,
                            T *__restrict__ out, const RhsScalars *rs, Geom g) {
-  const long long M = g.M, N = g.N, Next = g.Next;
-  const long long Nh1 = 4 * N, Nh2 = Nh1 + Next, Ndh1 = Nh2 + Next, Ndh2 = Ndh1 + Next;
-  const T inv_a2 = (T)(1.0 / rs->a2), two_inv_a2 = (T)(2.0 / rs->a2);
-  const T h3 = (T)(3.0 * rs->H), pm2 = (T)(2.0 * rs->p_mean);
-  const C2<T> *s0 = s, *s1 = s + M, *s2 = s + 2 * M, *s3 = s + 3 * M;
-  const C2<T> *s4 = s + 5 * M, *s5 = s + 6 * M;
+  const long long M = g.M;
+  const TensorConsts<T> tc(rs);
   const unsigned mz_magic = g.mz_magic;
   const int mz_shift = g.mz_shift, logny = g.logny;
   for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < M;
@@ -277,70 +235,47 @@ __global__ void k_update_h(const C2<T> *__restrict__ s, const T *__restrict__ y,
     m.j = (int)(r & (unsigned)(g.ny - 1));
     m.i = (int)(r >> logny);
     C2<T> n0 = mk2c<T>(0, 0), n1 = mk2c<T>(0, 0);
-    T ksq;
-    if (id != 0) {
-      T kx, ky, kz;
-      if constexpr (sizeof(T) == 8) {
-        kx = kxf_of(g, m.i);
-        ky = kyf_of(g, m.j);
-        kz = kzf_of(g, m.k);
-        ksq = ksq64(g, m.i, m.j, m.k);
-      } else {
-        kx = (float)g.kxu * (float)((m.i > g.nx / 2) ? (m.i - g.nx) : m.i);
-        ky = (float)g.kyu * (float)((m.j > g.ny / 2) ? (m.j - g.ny) : m.j);
-        kz = (float)g.kzu * (float)m.k;
-        int ia = (m.i > g.nx / 2) ? (g.nx - m.i) : m.i;
-        int ja = (m.j > g.ny / 2) ? (g.ny - m.j) : m.j;
-        ksq = (float)g.kz2 * (float)m.k * (float)m.k;
-        ksq += (float)g.kx2 * (float)ia * (float)ia;
-        ksq += (float)g.ky2 * (float)ja * (float)ja;
-      }
-      const T inv_ksq = (T)1.0 / ksq;
-      const T fx = kx * inv_ksq, fy = ky * inv_ksq, fz = kz * inv_ksq;
-      C2<T> v0 = s0[id], v1 = s1[id], v2 = s2[id], v3 = s3[id], v4 = s4[id], v5 = s5[id];
-#define CL(c, a, b) mk2c<T>(a.x c b.x, a.y c b.y)
-#define SC(f, a) mk2c<T>((f) * a.x, (f) * a.y)
-      C2<T> t1 = CL(+, CL(+, CL(+, SC(kx * fx, v0), SC(ky * fy, v3)), SC(kz * fz, v5)),
-                    SC((T)2.0, CL(+, CL(+, SC(kx * fy, v1), SC(kx * fz, v2)), SC(ky * fz, v4))));
-      C2<T> t2 = CL(+, CL(+, v0, v3), v5);
-      C2<T> S1 = CL(+, t1, t2), S2 = CL(-, t1, t2);
-      // |kz| > DBL_EPSILON and |ky| > DBL_EPSILON of toolbox.c:377, 382: the
-      // grid components are either exactly 0 or at least 2 pi / L
-      if (m.k != 0) {
-        C2<T> k1 = CL(+, CL(+, SC(kx, v0), SC(ky, v1)), SC(kz, v2));
-        C2<T> k2 = CL(+, CL(+, SC(kx, v1), SC(ky, v3)), SC(kz, v4));
-        n0 = CL(+, CL(-, v0, SC((T)2.0 * fx, k1)), SC((T)0.5, CL(+, SC(fx * kx, S1), S2)));
-        n1 = CL(+, CL(-, CL(-, v1, SC(fx, k2)), SC(fy, k1)), SC((T)0.5 * fx * ky, S1));
-      } else if (m.j != 0) {
-        C2<T> k1 = CL(+, CL(+, SC(kx, v0), SC(ky, v1)), SC(kz, v2));
-        C2<T> k3 = CL(+, CL(+, SC(kx, v2), SC(ky, v4)), SC(kz, v5));
-        n0 = CL(+, CL(-, v0, SC((T)2.0 * fx, k1)), SC((T)0.5, CL(+, SC(fx * kx, S1), S2)));
-        n1 = CL(+, CL(-, CL(-, v2, SC(fx, k3)), SC(fz, k1)), SC((T)0.5 * fx * kz, S1));
-      } else {
-        C2<T> k2 = CL(+, CL(+, SC(kx, v1), SC(ky, v3)), SC(kz, v4));
-        C2<T> k3 = CL(+, CL(+, SC(kx, v2), SC(ky, v4)), SC(kz, v5));
-        n0 = CL(+, CL(-, v3, SC((T)2.0 * fy, k2)), SC((T)0.5, CL(+, SC(fy * ky, S1), S2)));
-        n1 = CL(+, CL(-, CL(-, v4, SC(fy, k3)), SC(fz, k2)), SC((T)0.5 * fy * kz, S1));
-      }
-#undef CL
-#undef SC
-    } else {
-      ksq = 0;
+    T ksq = 0;
+    if (id != 0) {  // the zero mode has no sources (its spectra are not read)
+      const C2<T> v[6] = {s[id], s[M + id], s[2 * M + id], s[3 * M + id], s[5 * M + id],
+                          s[6 * M + id]};
+      const ModeK<T> q = mode_k<T>(g, m);
+      ksq = q.ksq;
+      tensor_sources<T>(m, q, v, n0, n1);
     }
-    const T tm = -(pm2 + ksq * inv_a2);
-    const long long i1 = 2 * id;
-    typedef C2<T> V;
-    const V *yv = reinterpret_cast<const V *>(y);
-    V *ov = reinterpret_cast<V *>(out);
-    const V h1 = yv[(Nh1 + i1) / 2], h2 = yv[(Nh2 + i1) / 2];
-    const V d1 = yv[(Ndh1 + i1) / 2], d2 = yv[(Ndh2 + i1) / 2];
-    ov[(Nh1 + i1) / 2] = d1;
-    ov[(Nh2 + i1) / 2] = d2;
-    ov[(Ndh1 + i1) / 2] = mk2c<T>(tm * h1.x - h3 * d1.x + two_inv_a2 * n0.x,
-                                  tm * h1.y - h3 * d1.y + two_inv_a2 * n0.y);
-    ov[(Ndh2 + i1) / 2] = mk2c<T>(tm * h2.x - h3 * d2.x + two_inv_a2 * n1.x,
-                                  tm * h2.y - h3 * d2.y + two_inv_a2 * n1.y);
+    tensor_eom<T>(g, id, n0, n1, ksq, tc, y, out);
   }
+}
+
+// The last forward x pass of the six S_ij spectra (arrays 0..3, 5, 6 of
+// spec; z and y passes done) and update_h, writing the tensor segments of
+// out: x passes then k_update_h, or the fused k_fft_x_tensor, as the
+// autotuner chose (Ctx::tensor_fused).
+int tensor_last_pass(Ctx *c, void *spec, const void *y, void *out) {
+  const Geom &g = c->g;
+  const long long M = g.M;
+  if (c->mixed) {
+    C2<float> *s = (C2<float> *)spec;
+    if (c->tensor_fused) return fft_x_tensor<float>(c, s, s + 5 * M, (const float *)y, (float *)out);
+    IH_TRY((fft_xy<float>(c, s, M, 4, 0, -1)));
+    IH_TRY((fft_xy<float>(c, s + 5 * M, M, 2, 0, -1)));
+  } else {
+    C2<double> *s = (C2<double> *)spec;
+    if (c->tensor_fused)
+      return fft_x_tensor<double>(c, s, s + 5 * M, (const double *)y, (double *)out);
+    IH_TRY((fft_xy<double>(c, s, M, 4, 0, -1)));
+    IH_TRY((fft_xy<double>(c, s + 5 * M, M, 2, 0, -1)));
+  }
+  const unsigned gm = grid_for(M, 256, 4);
+  prof_begin(c, KK_UPDATE_H);
+  if (c->mixed)
+    k_update_h<float><<<gm, 256, 0, c->stream>>>((const C2<float> *)spec, (const float *)y,
+                                                 (float *)out, c->rs, g);
+  else
+    k_update_h<double><<<gm, 256, 0, c->stream>>>((const C2<double> *)spec, (const double *)y,
+                                                  (double *)out, c->rs, g);
+  prof_end(c, KK_UPDATE_H, 6.0 * M * c->tsize * 2 + 8.0 * g.Next * c->tsize);
+  return check_launch(c, "k_update_h");
 }
 
 // ---------------------------------------------------------------------------
@@ -847,6 +782,10 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
   // the diagnostics stay those of the last RHS run with the output flag
   if (output == 1) c->have_output = 0;
   const int do_filter = (filter == 1) && c->p.enable_filter;
+  // without the filter and the output flag nothing needs the full spectrum
+  // of phi: the derivatives come from round trips along x and y on its z
+  // spectrum Z (spec[4]), the z parts from Z inside the fused z pass
+  const int use_rt = c->roundtrip && !do_filter && output != 1;
   const unsigned gm = grid_for(M, 256, 4);
   // 1. phihat (and with the filter: dphi, psi, dpsi spectra, mask, write back)
   if (do_filter) {
@@ -863,17 +802,24 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
     prof_end(c, KK_FILTER, (double)M * (9 + (output ? 1 : 0)) * sizeof(C2<T>) + (double)M * sizeof(T));
     IH_TRY(check_launch(c, "k_filter_spectra"));
     IH_TRY((fft_c2r<T>(c, spec, M, yfl, N, 4)));
+  } else if (use_rt) {
+    IH_TRY((fft_zr2c<T>(c, yfl, 0, spec + 4 * M, 0, 1)));
   } else {
     IH_TRY((fft_r2c<T>(c, yfl, 0, spec + 4 * M, 0, 1)));
   }
   if (output == 1) IH_TRY(output_pre<T>(c, y, do_filter));
-  // 2. derivative spectra + inverse x, inverse y
-  IH_TRY((fft_x_deriv4_inv<T>(c, spec + 4 * M, spec, M)));
-  IH_TRY((fft_xy<T>(c, spec, M, 4, 1, +1)));
+  // 2. derivative spectra in (x, y, kz): d/dx, d/dy, (d/dz), laplacian
+  if (use_rt) {
+    IH_TRY((fft_xy_roundtrip<T>(c, spec + 4 * M, spec, spec + 3 * M, 0)));
+    IH_TRY((fft_xy_roundtrip<T>(c, spec + 4 * M, spec + M, spec + 2 * M, 1)));
+  } else {
+    IH_TRY((fft_x_deriv4_inv<T>(c, spec + 4 * M, spec, M)));
+    IH_TRY((fft_xy<T>(c, spec, M, 4, 1, +1)));
+  }
   // 3. fused inverse z + pointwise + GW products forward z
   int nblk = 0;
   IH_TRY((fft_z_rhs_fused<T>(c, spec, yfl, y.sc, lap, p, output == 1 ? rho : nullptr, spec,
-                             c->p.enable_gw, c->partials, &nblk)));
+                             c->p.enable_gw, c->partials, &nblk, use_rt)));
   k_reduce_finish<<<1, 256, 0, c->stream>>>(c->partials, nblk, g, y.sc, k.sc, c->rs, c->mixed);
   IH_TRY(check_launch(c, "k_reduce_finish"));
   // 4. diagnostics that need <rho> and H
@@ -881,14 +827,10 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
   // 5. tensor modes
   if (c->p.enable_gw) {
     // S_ij spectra: spec[0..3] and spec[5..6]; forward y and x passes
+    // (batched: per-array y-then-x ordering measured slower, no L2 reuse)
     IH_TRY((fft_xy<T>(c, spec, M, 4, 1, -1)));
     IH_TRY((fft_xy<T>(c, spec + 5 * M, M, 2, 1, -1)));
-    IH_TRY((fft_xy<T>(c, spec, M, 4, 0, -1)));
-    IH_TRY((fft_xy<T>(c, spec + 5 * M, M, 2, 0, -1)));
-    prof_begin(c, KK_UPDATE_H);
-    k_update_h<T><<<gm, 256, 0, c->stream>>>(spec, yfl, kfl, c->rs, g);
-    prof_end(c, KK_UPDATE_H, 6.0 * M * sizeof(C2<T>) + 8.0 * g.Next * sizeof(T));
-    IH_TRY(check_launch(c, "k_update_h"));
+    IH_TRY(tensor_last_pass(c, spec, yfl, kfl));
   }
   // 6. phi/psi equations of motion
   prof_begin(c, KK_UPDATE_PHI_PSI);

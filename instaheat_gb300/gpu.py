@@ -154,6 +154,7 @@ def load(build_if_missing: bool = True):
     L.ih_fft_set_engine.argtypes = [vp, C.c_int, C.c_int]
     L.ih_fft_get_engine.argtypes = [vp, C.c_int]
     L.ih_graphs_enable.argtypes = [vp, C.c_int]
+    L.ih_rhs_roundtrip.argtypes = [vp, C.c_int]
     L.ih_ensemble_create.argtypes = [C.POINTER(Params), C.c_int, C.POINTER(vp)]
     L.ih_ensemble_destroy.argtypes = [vp]
     L.ih_ensemble_destroy.restype = None
@@ -340,7 +341,7 @@ class Context:
                 known = json.loads(path.read_text()).get(key)
             except ValueError:
                 known = None
-            if known:
+            if known and len(known.get("engines", ())) == len(self.engines()):
                 for p, e in enumerate(known["engines"]):
                     self.set_engine(p, e)
                 self._wisdom_report = "from wisdom: " + known["report"]
@@ -371,8 +372,16 @@ class Context:
         """Replay DOPRI853 tries and post-step RHS evaluations as CUDA graphs."""
         self._ck(self.L_.ih_graphs_enable(self.h, int(on)), "ih_graphs_enable")
 
+    def roundtrip(self, on=True):
+        """Derivatives of phi in RHS evaluations without the filter and output
+        flags from x and y round trips on its z spectrum (on, the default) or
+        from the full 3-D spectrum (off)."""
+        self._ck(self.L_.ih_rhs_roundtrip(self.h, int(on)), "ih_rhs_roundtrip")
+
     def engines(self):
-        return tuple(int(self.L_.ih_fft_get_engine(self.h, p)) for p in range(3))
+        """Engines of the x, y, fused x passes, the x, y round trips and the
+        form of the last tensor x pass (0 separate, 1 fused)."""
+        return tuple(int(self.L_.ih_fft_get_engine(self.h, p)) for p in range(6))
 
     @classmethod
     def _member(cls, handle, p: Params):

@@ -3,6 +3,7 @@ workload on one GPU -- the command the ncu captures under profiles/ use.
 
     python -m instaheat_gb300.profile_case --n 256 --prec mixed --rhs 3
     python -m instaheat_gb300.profile_case --n 256 --prec mixed --steps 2
+    python -m instaheat_gb300.profile_case --n 256 --prec mixed --rhs 2 --autotune
     python -m instaheat_gb300.profile_case --n 256 --dt-study 0,32,256,2048
 
 --dt-study runs 12 DOPRI853 steps of the FP64 form and of the mixed form
@@ -101,6 +102,8 @@ def main(argv=None):
     ap.add_argument("--etas", default="0,64,256", help="eta values of the GW accuracy study")
     ap.add_argument("--engine", type=int, default=None,
                     help="FFT engine of the x/y passes (0 Stockham .. 4 three-step)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="the autotuner's engines, kept in and reused from the FFT wisdom file")
     args = ap.parse_args(argv)
     if args.gw_accuracy > 0:
         gw_accuracy(args.n, args.gw_accuracy, [float(x) for x in args.etas.split(",")], args.rtol)
@@ -114,6 +117,8 @@ def main(argv=None):
         for p in range(3):
             if not (p == 2 and args.engine == gpu.FFT_THREESTEP):
                 ctx.set_engine(p, args.engine)
+    elif args.autotune:
+        print(ctx.autotune(wisdom=True), flush=True)
     ctx.ic(seed=0, amp=1e-3)
     ctx.dopri_init(gpu.dopri_cfg(args.rtol, args.rtol), 0.0, 1e-3)   # one filtered RHS
     for _ in range(args.rhs):

@@ -272,6 +272,81 @@ def test_rhs_engines_f64_parity(gpu_mod, oracle_mod, engine):
     assert max(errs.values()) < 1e-11, errs
 
 
+@pytest.mark.parametrize("rt_engine", [1, 2])  # two-step, two-step with 64-byte tiles
+@pytest.mark.parametrize("n,L", [((64, 32, 16), (20.0, 15.0, 12.0)),
+                                 ((128, 64, 8), (25.0, 10.0, 20.0)),
+                                 ((32, 32, 32), (20.0, 20.0, 30.0))])
+def test_rhs_roundtrip_f64_parity(gpu_mod, oracle_mod, n, L, rt_engine):
+    """RHS without the filter and output flags, whose derivatives come from
+    the x and y round trips on the z spectrum of phi: within 1e-11 of the
+    oracle for both round-trip engines, and so is the same RHS formed from
+    the full 3-D spectrum."""
+    ctx = gpu_mod.Context(n=n, L=L, precision=gpu_mod.PREC_F64)
+    ctx.set_engine(3, rt_engine)
+    ctx.set_engine(4, rt_engine)
+    assert ctx.engines()[3:5] == (rt_engine, rt_engine)
+    o = oracle_mod.Oracle(n=n, L=L)
+    f = make_state(o, seed=21)
+    r_ref, _ = o.rhs(f, filter=0)
+    r_rt, _ = ctx.mk_rhs(f, filter=0)
+    errs = seg_rel_err(r_rt, r_ref, o.N, o.Next)
+    assert max(errs.values()) < 1e-11, errs
+    ctx.roundtrip(False)
+    r_full, _ = ctx.mk_rhs(f, filter=0)
+    errs = seg_rel_err(r_full, r_ref, o.N, o.Next)
+    assert max(errs.values()) < 1e-11, errs
+
+
+@pytest.mark.parametrize("fused", [0, 1])
+@pytest.mark.parametrize("n,L", [((64, 32, 16), (20.0, 15.0, 12.0)), ((32, 32, 32), (20.0, 20.0, 20.0)),
+                                 ((128, 16, 8), (30.0, 10.0, 10.0))])
+@pytest.mark.parametrize("filt", [0, 1])
+def test_rhs_tensor_pass_forms_f64(gpu_mod, oracle_mod, n, L, fused, filt):
+    """The last tensor x pass as x passes + update_h (0) or as one kernel that
+    accumulates the TT projection spectrum by spectrum (1): the RHS within
+    1e-11 of the oracle either way."""
+    ctx = gpu_mod.Context(n=n, L=L, precision=gpu_mod.PREC_F64)
+    ctx.set_engine(5, fused)
+    assert ctx.engines()[5] == fused
+    o = oracle_mod.Oracle(n=n, L=L)
+    f = make_state(o, seed=23)
+    r_ref, _ = o.rhs(f, filter=filt)
+    r_gpu, _ = ctx.mk_rhs(f, filter=filt)
+    errs = seg_rel_err(r_gpu, r_ref, o.N, o.Next)
+    assert max(errs.values()) < 1e-11, errs
+
+
+def test_rhs_tensor_pass_forms_mixed_agree(gpu_mod, oracle_mod):
+    """Mixed form (FP32 transforms): both tensor x-pass forms agree within
+    FP32 rounding, 1e-5 of each tensor segment's magnitude."""
+    n = (256, 64, 32)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=24)
+    rs = []
+    for fused in (0, 1):
+        ctx.set_engine(5, fused)
+        rs.append(ctx.mk_rhs(f, filter=0)[0])
+    errs = seg_rel_err(rs[1], rs[0], o.N, o.Next)
+    assert max(errs[k] for k in ("h1", "h2", "dh1", "dh2")) < 1e-5, errs
+
+
+@pytest.mark.parametrize("n", [(64, 64, 64), (512, 16, 8)])
+def test_rhs_roundtrip_mixed_matches_full(gpu_mod, oracle_mod, n):
+    """Mixed form: the round-trip RHS and the full-spectrum RHS agree within
+    FP32 rounding (1e-5 of each segment's magnitude; a', through the FP32
+    gradient energy in <rho>, within 1e-10 as against the oracle)."""
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=22)
+    r_rt, _ = ctx.mk_rhs(f, filter=0)
+    ctx.roundtrip(False)
+    r_full, _ = ctx.mk_rhs(f, filter=0)
+    errs = seg_rel_err(r_rt, r_full, o.N, o.Next)
+    assert max(v for k, v in errs.items() if k != "a") < 1e-5, errs
+    assert errs["a"] < 1e-10, errs
+
+
 def test_autotune_picks_an_engine_and_keeps_parity(gpu_mod, oracle_mod):
     n = (64, 64, 64)
     ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
