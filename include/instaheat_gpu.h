@@ -183,7 +183,10 @@ const char *ih_autotune_report(const ih_context *c);
 /* Pin or read the engine of one pass: pass 0 = x, 1 = y, 2 = the fused
  * inverse x pass, 3 / 4 = the x / y derivative round trips (two-step forms
  * only), 5 = the last x pass of the tensor sources (0 = x passes then
- * update_h, 1 = one kernel accumulating the TT projection); engine IH_FFT_STOCKHAM, IH_FFT_TWOSTEP (register two-step,
+ * update_h, 1 = one kernel accumulating the TT projection), 6 = the fused z
+ * pass of the RHS (1 = the wide-row engine, 8 lanes x 16 values per row, where
+ * it applies: mixed form, nz = 256 -- the default; 0 = a warp per row);
+ * engine IH_FFT_STOCKHAM, IH_FFT_TWOSTEP (register two-step,
  * 128-byte tiles), IH_FFT_TWOSTEP_HALF (64-byte tiles), IH_FFT_PIPELINED
  * (register two-step in persistent CTAs that copy the next tile in with
  * cp.async while transforming the current one) or IH_FFT_THREESTEP (three

@@ -485,19 +485,21 @@ const char *ih_autotune_report(const ih_context *h) {
 
 int ih_fft_set_engine(ih_context *h, int pass, int engine) {
   CTX_CHECK(h);
-  if (pass < 0 || pass > 5 || engine < 0 || engine >= FV_COUNT) return IH_ERR_ARG;
+  if (pass < 0 || pass > 6 || engine < 0 || engine >= FV_COUNT) return IH_ERR_ARG;
   if (pass == 2 && engine == FV_THREESTEP) return IH_ERR_ARG;
   if ((pass == 3 || pass == 4) && engine != FV_TWOSTEP && engine != FV_TWOSTEP_HALF)
     return IH_ERR_ARG;
-  if (pass == 5 && engine > 1) return IH_ERR_ARG;
+  if (pass >= 5 && engine > 1) return IH_ERR_ARG;
   if (pass < 2) {
     h->c.xy_var[pass] = engine;
   } else if (pass == 2) {
     h->c.d4_var = engine;
   } else if (pass < 5) {
     h->c.rt_var[pass - 3] = engine;
-  } else {
+  } else if (pass == 5) {
     h->c.tensor_fused = engine;
+  } else {
+    h->c.zwide = engine;
   }
   h->c.graph_epoch += 1;
   return IH_OK;
@@ -517,9 +519,10 @@ int ih_graphs_enable(ih_context *h, int on) {
 }
 
 int ih_fft_get_engine(const ih_context *h, int pass) {
-  if (!h || pass < 0 || pass > 5) return -1;
+  if (!h || pass < 0 || pass > 6) return -1;
   if (pass < 2) return h->c.xy_var[pass];
   if (pass == 5) return h->c.tensor_fused;
+  if (pass == 6) return h->c.zwide;
   return pass == 2 ? h->c.d4_var : h->c.rt_var[pass - 3];
 }
 

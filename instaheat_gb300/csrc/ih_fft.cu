@@ -35,41 +35,11 @@
 #include <unordered_map>
 #include "ih_internal.cuh"
 #include "ih_tensor.cuh"
+#include "ih_fftcore.cuh"
 
 namespace ih {
 
-template <typename T>
-__device__ __forceinline__ C2<T> mk2(T x, T y) {
-  C2<T> r;
-  r.x = x;
-  r.y = y;
-  return r;
-}
-// complex helpers, templated on the vector type so that float2/double2 deduce
-template <typename V>
-__device__ __forceinline__ V cmul(V a, V b) {
-  V r;
-  r.x = a.x * b.x - a.y * b.y;
-  r.y = a.x * b.y + a.y * b.x;
-  return r;
-}
-template <typename V>
-__device__ __forceinline__ V cadd(V a, V b) {
-  V r;
-  r.x = a.x + b.x;
-  r.y = a.y + b.y;
-  return r;
-}
-template <typename V>
-__device__ __forceinline__ V csub(V a, V b) {
-  V r;
-  r.x = a.x - b.x;
-  r.y = a.y - b.y;
-  return r;
-}
-
 template <typename T> __host__ __device__ constexpr int tileB() { return 128 / (int)(2 * sizeof(T)); }
-__host__ __device__ constexpr int clog2(int v) { return v <= 1 ? 0 : 1 + clog2(v >> 1); }
 
 // L = R1 * R2: threads per pencil in step 1, points per thread in step 1
 template <int L> struct Fac;
@@ -104,81 +74,6 @@ template <int L> __device__ __forceinline__ int xrow(int r) {
   const int f = (a == b) ? (r >> a) : ((r >> a) ^ (r >> b));
   return r ^ (f & 1);
 }
-// exp(-2 pi i m/16) for a compile-time m: the cosines and sines of multiples
-// of pi/8 (cos pi/8, sin pi/8, sqrt(1/2)), correctly rounded in double
-template <typename T>
-__device__ __forceinline__ C2<T> w16(int m) {
-  constexpr double c = 0.92387953251128675613, s = 0.38268343236508977173,
-                   h = 0.70710678118654752440;
-  // a switch (not a table) so that a constant m folds to two literals
-  switch (m & 15) {
-    case 0: return mk2<T>((T)1, (T)0);
-    case 1: return mk2<T>((T)c, (T)-s);
-    case 2: return mk2<T>((T)h, (T)-h);
-    case 3: return mk2<T>((T)s, (T)-c);
-    case 4: return mk2<T>((T)0, (T)-1);
-    case 5: return mk2<T>((T)-s, (T)-c);
-    case 6: return mk2<T>((T)-h, (T)-h);
-    case 7: return mk2<T>((T)-c, (T)-s);
-    case 8: return mk2<T>((T)-1, (T)0);
-    case 9: return mk2<T>((T)-c, (T)s);
-    case 10: return mk2<T>((T)-h, (T)h);
-    case 11: return mk2<T>((T)-s, (T)c);
-    case 12: return mk2<T>((T)0, (T)1);
-    case 13: return mk2<T>((T)s, (T)c);
-    case 14: return mk2<T>((T)h, (T)h);
-    default: return mk2<T>((T)c, (T)s);
-  }
-}
-
-// bit reversal of K over BITS bits, as a compile-time constant
-template <int K, int BITS> struct Brev {
-  static constexpr int value = ((K & 1) << (BITS - 1)) | Brev<(K >> 1), BITS - 1>::value;
-};
-template <int K> struct Brev<K, 0> {
-  static constexpr int value = 0;
-};
-
-// v[k] <- v[brev(k)], every index a template constant (the registers are
-// renamed; nothing is staged in local memory)
-template <typename T, int R, int... K>
-__device__ __forceinline__ void brev_permute(C2<T> (&v)[R], std::integer_sequence<int, K...>) {
-  const C2<T> t[R] = {v[Brev<K, clog2(R)>::value]...};
-  ((v[K] = t[K]), ...);
-}
-
-// In-register DFT of R points: v[k] <- sum_n v[n] exp(sign 2 pi i nk/R).
-// Radix-2 decimation in frequency; the bit-reversed result order is undone by
-// a compile-time register permutation.  Twiddles are compile-time constants
-// for R <= 16, else tw[m * ts] = exp(-2 pi i m/R).
-template <typename T, int R>
-__device__ __forceinline__ void reg_dft(C2<T> (&v)[R], const C2<T> *tw, int ts, int sign) {
-  constexpr int LOGR = clog2(R);
-#pragma unroll
-  for (int s = 0; s < LOGR; ++s) {
-    const int len = R >> s, half = len >> 1;
-#pragma unroll
-    for (int st = 0; st < R; st += len) {
-#pragma unroll
-      for (int j = 0; j < half; ++j) {
-        const C2<T> a = v[st + j], b = v[st + j + half];
-        v[st + j] = cadd(a, b);
-        const C2<T> d = csub(a, b);
-        if (j == 0) {
-          v[st + j + half] = d;
-        } else if (4 * j == len) {  // exp(sign i pi/2) = sign * i
-          v[st + j + half] = mk2<T>(-(T)sign * d.y, (T)sign * d.x);
-        } else {
-          C2<T> w = (R <= 16) ? w16<T>(j * (16 / len)) : tw[j * (R / len) * ts];
-          if (sign > 0) w.y = -w.y;
-          v[st + j + half] = cmul(d, w);
-        }
-      }
-    }
-  }
-  brev_permute<T, R>(v, std::make_integer_sequence<int, R>{});
-}
-
 // exp(sign 2 pi i m / L) from the table exp(-2 pi i m/L)
 // Butterflies per thread per radix-4 stage (2K per radix-2 stage); the
 // launchers size CTAs so that B*L <= 4*K*nt.
@@ -584,25 +479,6 @@ __device__ __forceinline__ int lane_brev(int t, int lw) {
   return (int)(__brev((unsigned)t) >> (32 - lw));
 }
 
-// conjugate for the inverse direction (S = +1)
-template <int S, typename V>
-__device__ __forceinline__ V cj(V w) {
-  if (S > 0) w.y = -w.y;
-  return w;
-}
-template <typename V>
-__device__ __forceinline__ V shfl_xor_c(V v, int m) {
-  v.x = __shfl_xor_sync(0xffffffffu, v.x, m);
-  v.y = __shfl_xor_sync(0xffffffffu, v.y, m);
-  return v;
-}
-template <typename V>
-__device__ __forceinline__ V shfl_idx_c(V v, int src) {
-  v.x = __shfl_sync(0xffffffffu, v.x, src);
-  v.y = __shfl_sync(0xffffffffu, v.y, src);
-  return v;
-}
-
 // per-lane twiddles of the forward transform (the inverse conjugates them)
 template <typename T, int H> struct ZTw {
   using Gm = ZGeo<H>;
@@ -832,31 +708,6 @@ __global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_zc2r(const C2<T> *in, 
   }
 }
 
-// k components (setup.c:609-666).  FP64: the reference's expressions
-// (pars.x.k * i; k2 = pars.z.k2*k*k + pars.x.k2*i*i + pars.y.k2*j*j).
-// FP32: the same products in single precision.
-template <typename T>
-__device__ __forceinline__ T kfac(double unit, int n) {
-  if constexpr (sizeof(T) == 8) {
-    return unit * n;
-  } else {
-    return (float)unit * (float)n;
-  }
-}
-template <typename T>
-__device__ __forceinline__ T ksq(const Geom &g, int ia, int ja, int kz) {
-  if constexpr (sizeof(T) == 8) {
-    double q = g.kz2 * kz * kz;
-    q += g.kx2 * ia * ia;
-    q += g.ky2 * ja * ja;
-    return q;
-  } else {
-    float q = (float)g.kz2 * (float)kz * (float)kz;
-    q += (float)g.kx2 * (float)ia * (float)ia;
-    q += (float)g.ky2 * (float)ja * (float)ja;
-    return q;
-  }
-}
 
 // d/dx, d/dy, d/dz and laplacian spectra of phihat/N, inverse x transform each.
 // k vectors follow setup.c:609-666: first-derivative components are zero on
@@ -1110,10 +961,18 @@ __global__ void __launch_bounds__(pass_threads<L, B>(), 2) k_fft_x_deriv4_pipe(c
 // X[k2 + R2 k1] in registers.  The inverse starts from that layout: DFT_R1
 // over k1, twiddle w^(n1 k2), exchange, DFT_R2 over k2 -> x[n1 + R1 n2], the
 // step-1 thread layout again.  Two exchange buffers, one per output.
-template <typename T, int L, int B>
-__global__ void __launch_bounds__(pass_threads<L, B>()) k_fft_xy_rt(
+// ACC (the y round trip): out1 += the second derivative + (-kz^2) in / nz,
+// completing the laplacian of the x round trip; out1 and in are read again
+// (in from cache) just before the last exchange, at the positions the thread
+// writes.
+// resident CTAs asked of the register allocator: 16 warps per SM (FP32)
+template <typename T, int L, int B> __host__ __device__ constexpr int rt_min_blocks() {
+  return (sizeof(T) == 4 && 512 / pass_threads<L, B>() > 1) ? 512 / pass_threads<L, B>() : 1;
+}
+template <typename T, int L, int B, bool ACC>
+__global__ void __launch_bounds__(pass_threads<L, B>(), (rt_min_blocks<T, L, B>())) k_fft_xy_rt(
     const C2<T> *in, C2<T> *out0, C2<T> *out1, long long sj, long long so, int mz, double ku,
-    double k2u, double scale, const C2<T> *twg) {
+    double k2u, double scale, double kz2u, double invnz, const C2<T> *twg) {
   constexpr int R1 = Fac<L>::R1, R2 = Fac<L>::R2;
   constexpr int LB = clog2(B), P = B;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -1169,6 +1028,19 @@ __global__ void __launch_bounds__(pass_threads<L, B>()) k_fft_xy_rt(
         e[xrow<L>(q * R1 + n1) * P + b] = (n1 == 0) ? w[n1] : cmul(w[n1], twid(tw, (n1 * q) & (L - 1), +1));
     }
   }
+  C2<T> acc[R2];  // ACC: the x part in out1 + (-kz^2) in / nz
+  if constexpr (ACC) {
+    if (q < R1 && b < bv) {
+      const int kz = z0 + b;
+      const T f = -((T)kz2u * (T)kz * (T)kz) * (T)invnz;
+#pragma unroll
+      for (int n2 = 0; n2 < R2; ++n2) {
+        const long long i = off + (long long)(q + R1 * n2) * sj + b;
+        const C2<T> zv = in[i], lx = out1[i];
+        acc[n2] = mk2<T>(lx.x + f * zv.x, lx.y + f * zv.y);
+      }
+    }
+  }
   __syncthreads();
   if (q < R1) {  // q = n1
 #pragma unroll
@@ -1182,7 +1054,9 @@ __global__ void __launch_bounds__(pass_threads<L, B>()) k_fft_xy_rt(
       if (b < bv) {
 #pragma unroll
         for (int n2 = 0; n2 < R2; ++n2) {
-          dst[(long long)(q + R1 * n2) * sj + b] = v[n2];
+          C2<T> r = v[n2];
+          if (ACC && o == 1) r = cadd(r, acc[n2]);
+          dst[(long long)(q + R1 * n2) * sj + b] = r;
         }
       }
     }
@@ -1345,32 +1219,10 @@ __global__ void __launch_bounds__(L / 4 * B, (xt_min_blocks<T, L, B>())) k_fft_x
   }
 }
 
-// energy density and pressure at one point (see above)
-template <typename T, bool MIXED>
-__device__ __forceinline__ void rho_p(T dx, T dy, T dz, T phi, T dph, T ps, T inv_a2, T m2, T third,
-                                      T phib, T pib, T psib, T &rho, T &p) {
-  T grad = dx * dx;
-  grad += dy * dy;
-  grad += dz * dz;
-  if (!MIXED) {
-    T t1 = ((T)0.5 - ps) * dph * dph;
-    T t2 = ((T)0.5 + ps) * grad * inv_a2;
-    T V = m2 * phi * phi * (T)0.5;
-    rho = t1 + t2 + V;
-    p = t1 - t2 * third - V;
-  } else {
-    T pif = pib + dph;
-    T kin = ((T)0.5 - psib) * ((T)2.0 * pib * dph + dph * dph) - ps * pif * pif;
-    T grd = ((T)0.5 + psib + ps) * grad * inv_a2;
-    T pot = m2 * phib * phi + (T)0.5 * m2 * phi * phi;
-    rho = kin + grd + pot;
-    p = kin - grd * third - pot;
-  }
-}
 
 // ZSRC: the inputs are the round-trip outputs d/dx Z, d/dy Z (arrays 0, 1),
-// the y and x parts of the laplacian (arrays 2, 3) and Z itself (array 4); the
-// z derivative and the z part of the laplacian are applied to Z here.
+// the laplacian (array 3, completed by the y round trip) and Z itself (array
+// 4), from which the z derivative is formed here.
 // Otherwise arrays 0..3 hold the four full derivative spectra.
 template <typename T, bool MIXED, int H, bool ZSRC>
 __global__ void __launch_bounds__(32 * zwarps<T>(), (sizeof(T) == 4 && H <= 128 ? 3 : 1)) k_fft_z_rhs_fused(const C2<T> *d4, long long dstride, const T *yfl,
@@ -1399,11 +1251,9 @@ __global__ void __launch_bounds__(32 * zwarps<T>(), (sizeof(T) == 4 && H <= 128 
     for (int a = 0; a < 4; ++a) {
       C2<T> x[R], xH;
       if constexpr (ZSRC) {
-        // Z is fetched for a = 2 and again (from L1) for a = 3 rather than
-        // kept live across a transform
-        C2<T> zx[R], zH;
-        if (a >= 2) zc2r_fetch<T, H>(d4 + 4 * dstride + row * (H + 1), t, valid, zx, zH);
         if (a == 2) {  // i kz Z / nz, zero on the Nyquist index
+          C2<T> zx[R], zH;
+          zc2r_fetch<T, H>(d4 + 4 * dstride + row * (H + 1), t, valid, zx, zH);
 #pragma unroll
           for (int n = 0; n < R; ++n) {
             const T f = kfac<T>(g.kzu, t + W * n) * invnz;
@@ -1412,18 +1262,6 @@ __global__ void __launch_bounds__(32 * zwarps<T>(), (sizeof(T) == 4 && H <= 128 
           xH = mk2<T>(0, 0);
         } else {
           zc2r_fetch<T, H>(d4 + a * dstride + row * (H + 1), t, valid, x, xH);
-          if (a == 3) {  // x part (array 3) + y part (array 2) + (-kz^2) Z / nz
-            C2<T> yx[R], yH;
-            zc2r_fetch<T, H>(d4 + 2 * dstride + row * (H + 1), t, valid, yx, yH);
-#pragma unroll
-            for (int n = 0; n < R; ++n) {
-              const int kz = t + W * n;
-              const T f = -((T)g.kz2 * (T)kz * (T)kz) * invnz;
-              x[n] = mk2<T>(x[n].x + yx[n].x + f * zx[n].x, x[n].y + yx[n].y + f * zx[n].y);
-            }
-            const T fH = -((T)g.kz2 * (T)H * (T)H) * invnz;
-            xH = mk2<T>(xH.x + yH.x + fH * zH.x, xH.y + yH.y + fH * zH.y);
-          }
         }
       } else {
         zc2r_fetch<T, H>(d4 + a * dstride + row * (H + 1), t, valid, x, xH);
@@ -1810,10 +1648,18 @@ struct RTLaunch {
   int go(dim3 grid, long long sj, long long so, double ku, double k2u, double scale,
          const C2<T> *tw) {
     const size_t sm = sizeof(C2<T>) * ((size_t)L + 2 * (size_t)L * B);
-    cudaFuncSetAttribute(k_fft_xy_rt<T, L, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sm);
-    k_fft_xy_rt<T, L, B><<<grid, pass_threads<L, B>(), sm, c->stream>>>(
-        z, d1, d2, sj, so, c->g.mz, ku, k2u, scale, tw);
+    const double invnz = 1.0 / (double)c->g.nz;
+    if (axis == 1) {
+      cudaFuncSetAttribute(k_fft_xy_rt<T, L, B, true>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_fft_xy_rt<T, L, B, true><<<grid, pass_threads<L, B>(), sm, c->stream>>>(
+          z, d1, d2, sj, so, c->g.mz, ku, k2u, scale, c->g.kz2, invnz, tw);
+    } else {
+      cudaFuncSetAttribute(k_fft_xy_rt<T, L, B, false>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_fft_xy_rt<T, L, B, false><<<grid, pass_threads<L, B>(), sm, c->stream>>>(
+          z, d1, d2, sj, so, c->g.mz, ku, k2u, scale, c->g.kz2, invnz, tw);
+    }
     return IH_OK;
   }
   template <int L>
@@ -1876,7 +1722,7 @@ int fft_xy_roundtrip(Ctx *c, const C2<T> *z, C2<T> *d1, C2<T> *d2, int axis) {
   prof_begin(c, KK_XY_RT);
   IH_TRY(dispatch_len(axis == 0 ? g.nx : g.ny, RTLaunch<T>{c, z, d1, d2, axis, c->rt_var[axis]},
                       allow512<T>()));
-  prof_end(c, KK_XY_RT, 3.0 * g.M * sizeof(C2<T>));
+  prof_end(c, KK_XY_RT, (axis == 1 ? 4.0 : 3.0) * g.M * sizeof(C2<T>));
   return check_launch(c, "k_fft_xy_rt");
 }
 
@@ -1936,11 +1782,15 @@ int fft_z_rhs_fused(Ctx *c, const C2<T> *d4, const T *yfl, const double *ysc, T 
                     T *rho, C2<T> *s6, int gw, double *partials, int *nblocks_out, int zsrc) {
   const Geom &g = c->g;
   prof_begin(c, KK_Z_RHS_FUSED);
-  IH_TRY(dispatch_len(
-      g.h, FusedLaunch<T>{c, d4, yfl, ysc, lap, p, rho, s6, gw, partials, nblocks_out, zsrc},
-      false));
+  if (sizeof(T) == 4 && fused_wide_ok(c)) {  // nz = 256, mixed form: the wide-row engine
+    IH_TRY(fused_wide_launch(c, d4, yfl, ysc, lap, p, rho, s6, gw, partials, nblocks_out, zsrc));
+  } else {
+    IH_TRY(dispatch_len(
+        g.h, FusedLaunch<T>{c, d4, yfl, ysc, lap, p, rho, s6, gw, partials, nblocks_out, zsrc},
+        false));
+  }
   prof_end(c, KK_Z_RHS_FUSED,
-           (double)(4 + (zsrc ? 1 : 0) + (gw ? 6 : 0)) * g.M * sizeof(C2<T>) +
+           (double)(4 + (gw ? 6 : 0)) * g.M * sizeof(C2<T>) +
                (double)(3 + 2 + (rho ? 1 : 0)) * g.N * sizeof(T));
   return check_launch(c, "k_fft_z_rhs_fused");
 }
@@ -2027,8 +1877,8 @@ static int autotune_t(Ctx *c) {
         else if (pass == 2)
           st = fft_x_deriv4_inv<T>(c, sp + 4 * M, sp, M);
         else
-          st = fft_xy_roundtrip<T>(c, sp + 4 * M, sp + (pass - 3) * M, sp + (6 - pass) * M,
-                                   pass - 3);  // the RHS's arrays: d/dx 0, d2/dx2 3, d/dy 1, d2/dy2 2
+          st = fft_xy_roundtrip<T>(c, sp + 4 * M, sp + (pass - 3) * M, sp + 3 * M,
+                                   pass - 3);  // the RHS's arrays: d/dx 0, d/dy 1, laplacian 3
       }
       if (st != IH_OK) break;
       cudaEventRecord(e1, c->stream);

@@ -189,6 +189,7 @@ struct Ctx {
   int rt_var[2] = {FV_TWOSTEP_HALF, FV_TWOSTEP_HALF};  // x, y round trips (two-step forms)
   int roundtrip = 1;  // RHS without filter/output: round trips instead of full spectra
   int tensor_fused = 0;  // update_h fused into the last x pass (autotuner's choice)
+  int zwide = 1;         // the wide-row fused z pass where it applies (nz = 256, mixed)
   std::string tune_report;
 };
 
@@ -245,7 +246,8 @@ int fft_x_deriv4_inv(Ctx *c, const C2<T> *phihat, C2<T> *out,
                      long long out_stride);
 // Round trips along x (axis 0) and y (axis 1) on the z spectra Z of phi:
 // d1 = IFFT(i k FFT(Z)) / (L nz), d2 = IFFT(-k^2 FFT(Z)) / (L nz), the
-// per-axis derivative spectra of the fused z pass.
+// per-axis derivative spectra of the fused z pass; the y round trip adds its
+// d2 and -kz^2 Z / nz to d2 (the x round trip's), completing the laplacian.
 template <typename T>
 int fft_xy_roundtrip(Ctx *c, const C2<T> *z, C2<T> *d1, C2<T> *d2, int axis);
 // The forward x pass of the six S_ij spectra (arrays 0..3 at s03, 4..5 at
@@ -257,12 +259,17 @@ int fft_x_tensor(Ctx *c, const C2<T> *s03, const C2<T> *s45, const T *y, T *out)
 // then per point (grad phi)^2, rho, p (and their FP64 block sums), writes the
 // laplacian and p (and rho), and when gw the six products d_i phi d_j phi
 // transformed forward along z into six half spectra.  zsrc: the inputs are
-// the round-trip outputs (d/dx, d/dy, y and x laplacian parts, Z in the
-// arrays 0..4), and d/dz and the z part of the laplacian come from Z.
+// the round-trip outputs (d/dx, d/dy, laplacian, Z in the arrays 0, 1, 3,
+// 4), and d/dz comes from Z.
 template <typename T>
 int fft_z_rhs_fused(Ctx *c, const C2<T> *d4, const T *yfl, const double *ysc,
                     T *lap, T *p, T *rho, C2<T> *s6, int gw, double *partials,
                     int *nblocks_out, int zsrc);
+// The same pass on the wide-row engine (ih_zwide.cu): mixed form, nz = 256.
+bool fused_wide_ok(const Ctx *c);
+int fused_wide_launch(Ctx *c, const void *d4, const void *yfl, const double *ysc, void *lap,
+                      void *p, void *rho, void *s6, int gw, double *partials, int *nblk_out,
+                      int zsrc);
 
 int fft_tables(Ctx *c);
 // time every engine variant of the x/y passes and the fused x pass on the

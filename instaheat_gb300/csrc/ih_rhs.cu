@@ -811,7 +811,7 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
   // 2. derivative spectra in (x, y, kz): d/dx, d/dy, (d/dz), laplacian
   if (use_rt) {
     IH_TRY((fft_xy_roundtrip<T>(c, spec + 4 * M, spec, spec + 3 * M, 0)));
-    IH_TRY((fft_xy_roundtrip<T>(c, spec + 4 * M, spec + M, spec + 2 * M, 1)));
+    IH_TRY((fft_xy_roundtrip<T>(c, spec + 4 * M, spec + M, spec + 3 * M, 1)));
   } else {
     IH_TRY((fft_x_deriv4_inv<T>(c, spec + 4 * M, spec, M)));
     IH_TRY((fft_xy<T>(c, spec, M, 4, 1, +1)));

@@ -379,9 +379,10 @@ class Context:
         self._ck(self.L_.ih_rhs_roundtrip(self.h, int(on)), "ih_rhs_roundtrip")
 
     def engines(self):
-        """Engines of the x, y, fused x passes, the x, y round trips and the
-        form of the last tensor x pass (0 separate, 1 fused)."""
-        return tuple(int(self.L_.ih_fft_get_engine(self.h, p)) for p in range(6))
+        """Engines of the x, y, fused x passes, the x, y round trips, the form
+        of the last tensor x pass (0 separate, 1 fused) and of the fused z pass
+        (1 wide rows where they apply, 0 a warp per row)."""
+        return tuple(int(self.L_.ih_fft_get_engine(self.h, p)) for p in range(7))
 
     @classmethod
     def _member(cls, handle, p: Params):

@@ -331,6 +331,39 @@ def test_rhs_tensor_pass_forms_mixed_agree(gpu_mod, oracle_mod):
     assert max(errs[k] for k in ("h1", "h2", "dh1", "dh2")) < 1e-5, errs
 
 
+@pytest.mark.parametrize("filt", [0, 1])
+def test_rhs_wide_z_pass_256(gpu_mod, oracle_mod, filt):
+    """nz = 256 in the mixed form runs the fused z pass on the wide-row
+    engine (8 lanes x 16 values per row): against the FP64 oracle the
+    fluctuation part of each real-space RHS segment within 1e-5 of its
+    magnitude, the tensor segments within 1e-4 (measured 2.6e-5 on dh1 for
+    both engines: FP32 transforms of the quadratic sources on 256^3), a'
+    within 5e-9 (measured 6.3e-10 unfiltered, 2.2e-9 filtered, for both
+    engines: the FP32 gradient energy in <rho>); the warp-per-row engine
+    agrees with it within 2e-5."""
+    n = (256, 256, 256)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
+    assert ctx.engines()[6] == 1
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=25)
+    r_ref, _ = o.rhs(f, filter=filt)
+    r_wide, _ = ctx.mk_rhs(f, filter=filt)
+    ctx.set_engine(6, 0)
+    r_warp, _ = ctx.mk_rhs(f, filter=filt)
+    N = o.N
+    for r_gpu in (r_wide, r_warp):
+        for s in range(4):
+            ref = r_ref[s * N:(s + 1) * N]
+            got = r_gpu[s * N:(s + 1) * N]
+            fl = np.abs((got - got.mean()) - (ref - ref.mean())).max()
+            assert fl <= 1e-5 * np.abs(ref - ref.mean()).max(), s
+        errs = seg_rel_err(r_gpu, r_ref, o.N, o.Next)
+        assert max(errs[k] for k in ("h1", "h2", "dh1", "dh2")) < 1e-4, errs
+        assert errs["a"] < 5e-9, errs
+    errs = seg_rel_err(r_wide, r_warp, o.N, o.Next)
+    assert max(errs[k] for k in ("dphi", "dpsi", "h1", "h2", "dh1", "dh2")) < 2e-5, errs
+
+
 @pytest.mark.parametrize("n", [(64, 64, 64), (512, 16, 8)])
 def test_rhs_roundtrip_mixed_matches_full(gpu_mod, oracle_mod, n):
     """Mixed form: the round-trip RHS and the full-spectrum RHS agree within
