@@ -201,6 +201,16 @@ int ih_fft_get_engine(const ih_context *c, int pass);
  * 3-D spectrum as the filtered / output RHS does.  The two agree to
  * rounding. */
 int ih_rhs_roundtrip(ih_context *c, int on);
+/* DOPRI853 stage fusion (no reference counterpart; off by default): the RHS
+ * evaluation of stage s also forms the input of stage s+1 (y + dt sum_j
+ * a_(s+1)j k_j, dopri853.c:340-436) while it writes k_s, instead of a
+ * separate combination pass that reads k_s back.  Same arithmetic in the same
+ * order: results are identical to the bit either way.  It applies with the
+ * separate form of the last tensor x pass (ih_fft_set_engine pass 5 = 0, the
+ * autotuner's usual choice).  It saves a read of k_s per stage but the
+ * update kernels that take on the combination stream up to 40 arrays at once
+ * and run below the separate pass's bandwidth: at 256^3 it is slower. */
+int ih_stage_fusion(ih_context *c, int on);
 
 /* CUDA graphs (no reference counterpart): each DOPRI853 try (its 11 stage
  * combinations and RHS evaluations, the final combination and the error

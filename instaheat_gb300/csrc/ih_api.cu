@@ -505,6 +505,13 @@ int ih_fft_set_engine(ih_context *h, int pass, int engine) {
   return IH_OK;
 }
 
+int ih_stage_fusion(ih_context *h, int on) {
+  CTX_CHECK(h);
+  h->c.stage_fusion = on ? 1 : 0;
+  h->c.graph_epoch += 1;
+  return IH_OK;
+}
+
 int ih_rhs_roundtrip(ih_context *h, int on) {
   CTX_CHECK(h);
   h->c.roundtrip = on ? 1 : 0;
@@ -877,6 +884,7 @@ int ih_ensemble_autotune(ih_ensemble *e) {
       c->rt_var[0] = twin->rt_var[0];
       c->rt_var[1] = twin->rt_var[1];
       c->tensor_fused = twin->tensor_fused;
+      c->zwide = twin->zwide;
       c->tune_report = twin->tune_report;
       c->graph_epoch += 1;
     } else {

@@ -1105,10 +1105,10 @@ template <typename T> constexpr size_t xt_smem(int L, int B) {
   return sizeof(C2<T>) * ((size_t)L + 2 * (size_t)L * B);
 }
 
-template <typename T, int L, int B>
+template <typename T, int L, int B, bool NEXT>
 __global__ void __launch_bounds__(L / 4 * B, (xt_min_blocks<T, L, B>())) k_fft_x_tensor(
-    const C2<T> *s03, const C2<T> *s45, long long astride, const T *__restrict__ y,
-    T *__restrict__ out, const RhsScalars *rs, Geom g, const C2<T> *twg) {
+    const C2<T> *s03, const C2<T> *s45, long long astride, T *y, T *__restrict__ out,
+    const RhsScalars *rs, Geom g, const C2<T> *twg, const NextLin nl) {
   constexpr int Q = L / 4, LB = clog2(B);
   constexpr bool R2F = (clog2(L) & 1) != 0;
   constexpr int NS0 = R2F ? 2 : 4;                                   // span after the first stage
@@ -1207,14 +1207,15 @@ __global__ void __launch_bounds__(L / 4 * B, (xt_min_blocks<T, L, B>())) k_fft_x
   }
   if (b < bv) {
     const TensorConsts<T> tc(rs);
+    const T dt = NEXT ? (T)*nl.dt : (T)0;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       m.i = j + r * Q;
       const long long id = (long long)m.i * sj + off + b;
       const T ksq = mode_k<T>(g, m).ksq;
       const C2<T> zero = mk2<T>(0, 0);
-      tensor_eom<T>(g, id, id != 0 ? n0[r] : zero, id != 0 ? n1[r] : zero, id != 0 ? ksq : (T)0,
-                    tc, y, out);
+      tensor_eom<T, NEXT>(g, id, id != 0 ? n0[r] : zero, id != 0 ? n1[r] : zero,
+                          id != 0 ? ksq : (T)0, tc, y, out, nl, dt);
     }
   }
 }
@@ -1688,31 +1689,43 @@ template <typename T>
 struct XTLaunch {
   Ctx *c;
   const C2<T> *s03, *s45;
-  const T *y;
+  T *y;
   T *out;
+  const NextLin *next;
+  template <int L, bool NEXT>
+  void go() {
+    constexpr int B = tensor_tile<T>();
+    const Geom &g = c->g;
+    const size_t sm = xt_smem<T>(L, B);
+    cudaFuncSetAttribute(k_fft_x_tensor<T, L, B, NEXT>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const NextLin nl = next ? *next : NextLin{};
+    k_fft_x_tensor<T, L, B, NEXT><<<dim3((g.mz + B - 1) / B, g.ny, 1), L / 4 * B, sm,
+                                     c->stream>>>(s03, s45, g.M, y, out, c->rs, g,
+                                                  tab<T>(c->tw_x), nl);
+  }
   template <int L>
   int run() {
     if constexpr (L == 512 && !allow512<T>()) {
       return IH_ERR_ARG;
     } else {
-      constexpr int B = tensor_tile<T>();
-      const Geom &g = c->g;
-      const size_t sm = xt_smem<T>(L, B);
-      cudaFuncSetAttribute(k_fft_x_tensor<T, L, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)sm);
-      k_fft_x_tensor<T, L, B><<<dim3((g.mz + B - 1) / B, g.ny, 1), L / 4 * B, sm, c->stream>>>(
-          s03, s45, g.M, y, out, c->rs, g, tab<T>(c->tw_x));
+      if (next)
+        go<L, true>();
+      else
+        go<L, false>();
       return IH_OK;
     }
   }
 };
 
 template <typename T>
-int fft_x_tensor(Ctx *c, const C2<T> *s03, const C2<T> *s45, const T *y, T *out) {
+int fft_x_tensor(Ctx *c, const C2<T> *s03, const C2<T> *s45, T *y, T *out,
+                 const NextLin *next) {
   const Geom &g = c->g;
   prof_begin(c, KK_X_TENSOR);
-  IH_TRY(dispatch_len(g.nx, XTLaunch<T>{c, s03, s45, y, out}, allow512<T>()));
-  prof_end(c, KK_X_TENSOR, 6.0 * g.M * sizeof(C2<T>) + 8.0 * g.Next * sizeof(T));
+  IH_TRY(dispatch_len(g.nx, XTLaunch<T>{c, s03, s45, y, out, next}, allow512<T>()));
+  prof_end(c, KK_X_TENSOR,
+           6.0 * g.M * sizeof(C2<T>) + (8.0 + (next ? 4.0 * (next->n + 2) : 0.0)) * g.Next * sizeof(T));
   return check_launch(c, "k_fft_x_tensor");
 }
 
@@ -1911,7 +1924,7 @@ static int autotune_t(Ctx *c) {
     float ms = 0.f;
     for (int r = 0; r <= reps && st == IH_OK; ++r) {
       if (r == 1) cudaEventRecord(e0, c->stream);
-      st = tensor_last_pass(c, sp, c->y.fl, c->ytmp.fl);
+      st = tensor_last_pass(c, sp, c->y.fl, c->ytmp.fl, nullptr);
     }
     if (st != IH_OK) break;
     cudaEventRecord(e1, c->stream);
@@ -1955,7 +1968,7 @@ int fft_autotune(Ctx *c) {
   template int fft_z_rhs_fused<T>(Ctx *, const C2<T> *, const T *, const double *, T *, T *,    \
                                   T *, C2<T> *, int, double *, int *, int);                     \
   template int fft_xy_roundtrip<T>(Ctx *, const C2<T> *, C2<T> *, C2<T> *, int);              \
-  template int fft_x_tensor<T>(Ctx *, const C2<T> *, const C2<T> *, const T *, T *);
+  template int fft_x_tensor<T>(Ctx *, const C2<T> *, const C2<T> *, T *, T *, const NextLin *);
 IH_INST(float)
 IH_INST(double)
 #undef IH_INST

@@ -72,6 +72,26 @@ struct Vec {                    // one state-shaped vector
   double *sc = nullptr;         // double[kSc] (device)
 };
 
+// Terms of a DOPRI853/RK4 stage combination (dopri853.c:340-436).
+constexpr int kMaxTerms = 12;
+// The next stage's input formed by the kernels that write the stage being
+// evaluated (k_s): out = base + dt (sum_j coef_j k_j + self k_s), the terms
+// in the order of the stand-alone combination (so the result is the same to
+// the bit), in place of the RHS input (out is the y the RHS reads: every
+// element is read before it is overwritten, by the same thread).
+struct NextLin {
+  const void *k[kMaxTerms];       // T[Nf] of the earlier stages with a nonzero coefficient
+  const double *ksc[kMaxTerms];   // their homogeneous parts
+  double coef[kMaxTerms];
+  float coeff[kMaxTerms];         // coef rounded to FP32 (the mixed form's fluctuation arithmetic)
+  int n;
+  double self;                    // the coefficient of k_s (0: none)
+  float selff;
+  const void *base;               // the step's start state (T[Nf])
+  const double *basesc;
+  const double *dt;               // the step size (device memory)
+};
+
 // kernel kinds for per-kernel timing and algorithmic-byte accounting
 enum KernelKind {
   KK_FFT_XY = 0,        // complex pass along x or y
@@ -190,6 +210,7 @@ struct Ctx {
   int roundtrip = 1;  // RHS without filter/output: round trips instead of full spectra
   int tensor_fused = 0;  // update_h fused into the last x pass (autotuner's choice)
   int zwide = 1;         // the wide-row fused z pass where it applies (nz = 256, mixed)
+  int stage_fusion = 0;  // DOPRI853 stage inputs formed by the RHS of the previous stage
   std::string tune_report;
 };
 
@@ -254,7 +275,8 @@ int fft_xy_roundtrip(Ctx *c, const C2<T> *z, C2<T> *d1, C2<T> *d2, int axis);
 // s45, stride M; z and y passes done) fused with update_h: writes the tensor
 // segments of out from those of y (toolbox.c:311-346, 363-397).
 template <typename T>
-int fft_x_tensor(Ctx *c, const C2<T> *s03, const C2<T> *s45, const T *y, T *out);
+int fft_x_tensor(Ctx *c, const C2<T> *s03, const C2<T> *s45, T *y, T *out,
+                 const NextLin *next);
 // Fused last inverse z pass for the RHS: c2r of the four derivative spectra,
 // then per point (grad phi)^2, rho, p (and their FP64 block sums), writes the
 // laplacian and p (and rho), and when gw the six products d_i phi d_j phi
@@ -278,10 +300,11 @@ int fft_autotune(Ctx *c);
 
 // ---------------------------------------------------------------------------
 // RHS and helpers (ih_rhs.cu)
-// the last forward x pass of the six S_ij spectra + update_h (either form)
-int tensor_last_pass(Ctx *c, void *spec, const void *y, void *out);
+// the last forward x pass of the six S_ij spectra + update_h (either form);
+// next: also form the tensor segments of the next stage input (in y)
+int tensor_last_pass(Ctx *c, void *spec, void *y, void *out, const NextLin *next);
 int rhs(Ctx *c, double t, Vec &y, Vec &k, int filter, int output,
-        const Vec *smry_src);
+        const Vec *smry_src, const NextLin *next = nullptr);
 int reduce_mean(Ctx *c, const void *arr, long long n, double *dev_out);
 int reduce_mean_f64(Ctx *c, const double *arr, long long n, double *dev_out);
 // variance of n device doubles around `mean` (toolbox.c:744-754) into

@@ -179,12 +179,44 @@ __global__ void k_reduce_finish(const double *partials, int nblk, Geom g,
 }
 
 // update_phi_psi (toolbox.c:282-299); mixed form: fluctuation parts only,
-// the homogeneous parts were written by k_reduce_finish.
-template <typename T, bool MIXED>
-__global__ void k_update_phi_psi(const T *__restrict__ y, const double *ysc,
-                                 const T *__restrict__ lap, const T *__restrict__ p,
-                                 T *__restrict__ out, const RhsScalars *rs,
-                                 long long N, double mass) {
+// the homogeneous parts were written by k_reduce_finish.  W points per
+// thread (one 16-byte vector per array).  NEXT: also the next stage's input
+// (nl) at the four real segments, written over y -- each element of y is
+// read, then overwritten, by the same thread.
+template <typename T> struct VecW;
+template <> struct VecW<float> {
+  using V = float4;
+  static constexpr int W = 4;
+};
+template <> struct VecW<double> {
+  using V = double2;
+  static constexpr int W = 2;
+};
+template <typename T>
+__device__ __forceinline__ void ld_w(const T *p, T (&v)[VecW<T>::W]) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 q = *reinterpret_cast<const float4 *>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+  } else {
+    const double2 q = *reinterpret_cast<const double2 *>(p);
+    v[0] = q.x; v[1] = q.y;
+  }
+}
+template <typename T>
+__device__ __forceinline__ void st_w(T *p, const T (&v)[VecW<T>::W]) {
+  if constexpr (sizeof(T) == 4) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  } else {
+    *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+  }
+}
+
+template <typename T, bool MIXED, bool NEXT>
+__global__ void k_update_phi_psi(T *y, const double *ysc, const T *__restrict__ lap,
+                                 const T *__restrict__ p, T *__restrict__ out,
+                                 const RhsScalars *rs, long long N, double mass,
+                                 const NextLin nl) {
+  constexpr int W = VecW<T>::W;
   const double a2d = rs->a2, Hd = rs->H, pmd = rs->p_mean;
   const T inv_a2 = (T)(1.0 / a2d), H = (T)Hd, h3 = (T)(3.0 * Hd), pm = (T)pmd;
   const T m2 = (T)(mass * mass);
@@ -195,33 +227,88 @@ __global__ void k_update_phi_psi(const T *__restrict__ y, const double *ysc,
     psib = (T)ysc[2];
     dpsib = (T)ysc[3];
   }
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
-       i += (long long)gridDim.x * blockDim.x) {
-    T ph = y[i], dph = y[N + i], ps = y[2 * N + i], dps = y[3 * N + i];
-    T l = lap[i], pp = p[i];
-    out[i] = dph;
-    out[2 * N + i] = dps;
-    if (!MIXED) {
-      out[N + i] = ((T)1.0 + (T)4.0 * ps) * l * inv_a2 - (h3 - (T)4.0 * dps) * dph -
-                   ((T)1.0 + (T)2.0 * ps) * (m2 * ph);
-      out[3 * N + i] = (T)0.5 * pp + (ps - (T)0.5) * pm - (T)4.0 * H * dps;
-    } else {
-      T psf = psib + ps, dpsf = dpsib + dps;
-      out[N + i] = ((T)1.0 + (T)4.0 * psf) * l * inv_a2 + (T)4.0 * dps * pib -
-                   (h3 - (T)4.0 * dpsf) * dph - (T)2.0 * ps * m2 * phib -
-                   ((T)1.0 + (T)2.0 * psf) * m2 * ph;
-      out[3 * N + i] = (T)0.5 * pp + ps * pm - (T)4.0 * H * dps;
+  const T dt = NEXT ? (T)*nl.dt : (T)0;
+  const long long nv = N / W;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
+       v += (long long)gridDim.x * blockDim.x) {
+    const long long i0 = v * W;
+    T ph[W], dph[W], ps[W], dps[W], l[W], pp[W], o1[W], o3[W];
+    ld_w<T>(y + i0, ph);
+    ld_w<T>(y + N + i0, dph);
+    ld_w<T>(y + 2 * N + i0, ps);
+    ld_w<T>(y + 3 * N + i0, dps);
+    ld_w<T>(lap + i0, l);
+    ld_w<T>(p + i0, pp);
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      if (!MIXED) {
+        o1[w] = ((T)1.0 + (T)4.0 * ps[w]) * l[w] * inv_a2 - (h3 - (T)4.0 * dps[w]) * dph[w] -
+                ((T)1.0 + (T)2.0 * ps[w]) * (m2 * ph[w]);
+        o3[w] = (T)0.5 * pp[w] + (ps[w] - (T)0.5) * pm - (T)4.0 * H * dps[w];
+      } else {
+        T psf = psib + ps[w], dpsf = dpsib + dps[w];
+        o1[w] = ((T)1.0 + (T)4.0 * psf) * l[w] * inv_a2 + (T)4.0 * dps[w] * pib -
+                (h3 - (T)4.0 * dpsf) * dph[w] - (T)2.0 * ps[w] * m2 * phib -
+                ((T)1.0 + (T)2.0 * psf) * m2 * ph[w];
+        o3[w] = (T)0.5 * pp[w] + ps[w] * pm - (T)4.0 * H * dps[w];
+      }
+    }
+    st_w<T>(out + i0, dph);
+    st_w<T>(out + N + i0, o1);
+    st_w<T>(out + 2 * N + i0, dps);
+    st_w<T>(out + 3 * N + i0, o3);
+    if constexpr (NEXT) {
+#pragma unroll
+      for (int seg = 0; seg < 4; ++seg) {
+        const T *o = seg == 0 ? dph : seg == 1 ? o1 : seg == 2 ? dps : o3;
+        const long long e = seg * N + i0;
+        T acc[W], x[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) acc[w] = 0;
+#pragma unroll
+        for (int j = 0; j < kMaxTerms; ++j) {
+          if (j < nl.n) {
+            ld_w<T>(reinterpret_cast<const T *>(nl.k[j]) + e, x);
+            const T cj = nl_coef<T>(nl, j);
+#pragma unroll
+            for (int w = 0; w < W; ++w) acc[w] += cj * x[w];
+          }
+        }
+        const T cs = nl_self<T>(nl);
+#pragma unroll
+        for (int w = 0; w < W; ++w) acc[w] += cs * o[w];
+        ld_w<T>(reinterpret_cast<const T *>(nl.base) + e, x);
+#pragma unroll
+        for (int w = 0; w < W; ++w) x[w] = x[w] + dt * acc[w];
+        st_w<T>(y + e, x);
+      }
     }
   }
 }
 
+// the homogeneous parts of the next stage input (after every kernel that
+// reads those of the current one): outsc = basesc + dt (sum_j coef_j ksc_j +
+// self ksc), in the order of the stand-alone combination
+__global__ void k_next_sc(const NextLin nl, const double *ksc, double *outsc) {
+  const int s = threadIdx.x;
+  if (s >= 5) return;
+  const double dt = *nl.dt;
+  double acc = 0.0;
+  for (int j = 0; j < nl.n; ++j) acc += nl.coef[j] * nl.ksc[j][s];
+  acc += nl.self * ksc[s];
+  outsc[s] = nl.basesc[s] + dt * acc;
+}
+
 // update_h with the TT projection (toolbox.c:311-346, 363-397).  s holds the
 // six S_ij spectra, spectra 4 and 5 at s + 5M.
-template <typename T>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 5 : 2)) k_update_h(const C2<T> *__restrict__ s, const T *__restrict__ y,
-                           T *__restrict__ out, const RhsScalars *rs, Geom g) {
+// NEXT: also the next stage's input at the tensor entries of y (nl).
+template <typename T, bool NEXT>
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (NEXT ? 3 : 5) : 2)) k_update_h(
+    const C2<T> *__restrict__ s, T *y, T *__restrict__ out, const RhsScalars *rs, Geom g,
+    const NextLin nl) {
   const long long M = g.M;
   const TensorConsts<T> tc(rs);
+  const T dt = NEXT ? (T)*nl.dt : (T)0;
   const unsigned mz_magic = g.mz_magic;
   const int mz_shift = g.mz_shift, logny = g.logny;
   for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < M;
@@ -243,39 +330,38 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 5 : 2)) k_update_h(cons
       ksq = q.ksq;
       tensor_sources<T>(m, q, v, n0, n1);
     }
-    tensor_eom<T>(g, id, n0, n1, ksq, tc, y, out);
+    tensor_eom<T, NEXT>(g, id, n0, n1, ksq, tc, y, out, nl, dt);
   }
 }
 
 // The last forward x pass of the six S_ij spectra (arrays 0..3, 5, 6 of
 // spec; z and y passes done) and update_h, writing the tensor segments of
 // out: x passes then k_update_h, or the fused k_fft_x_tensor, as the
-// autotuner chose (Ctx::tensor_fused).
-int tensor_last_pass(Ctx *c, void *spec, const void *y, void *out) {
+// autotuner chose (Ctx::tensor_fused).  next: the tensor entries of the next
+// stage input too (in y).
+template <typename T>
+static int tensor_last_pass_t(Ctx *c, C2<T> *s, T *y, T *out, const NextLin *next) {
   const Geom &g = c->g;
   const long long M = g.M;
-  if (c->mixed) {
-    C2<float> *s = (C2<float> *)spec;
-    if (c->tensor_fused) return fft_x_tensor<float>(c, s, s + 5 * M, (const float *)y, (float *)out);
-    IH_TRY((fft_xy<float>(c, s, M, 4, 0, -1)));
-    IH_TRY((fft_xy<float>(c, s + 5 * M, M, 2, 0, -1)));
-  } else {
-    C2<double> *s = (C2<double> *)spec;
-    if (c->tensor_fused)
-      return fft_x_tensor<double>(c, s, s + 5 * M, (const double *)y, (double *)out);
-    IH_TRY((fft_xy<double>(c, s, M, 4, 0, -1)));
-    IH_TRY((fft_xy<double>(c, s + 5 * M, M, 2, 0, -1)));
-  }
+  if (c->tensor_fused) return fft_x_tensor<T>(c, s, s + 5 * M, y, out, next);
+  IH_TRY((fft_xy<T>(c, s, M, 4, 0, -1)));
+  IH_TRY((fft_xy<T>(c, s + 5 * M, M, 2, 0, -1)));
   const unsigned gm = grid_for(M, 256, 4);
   prof_begin(c, KK_UPDATE_H);
-  if (c->mixed)
-    k_update_h<float><<<gm, 256, 0, c->stream>>>((const C2<float> *)spec, (const float *)y,
-                                                 (float *)out, c->rs, g);
-  else
-    k_update_h<double><<<gm, 256, 0, c->stream>>>((const C2<double> *)spec, (const double *)y,
-                                                  (double *)out, c->rs, g);
-  prof_end(c, KK_UPDATE_H, 6.0 * M * c->tsize * 2 + 8.0 * g.Next * c->tsize);
+  if (next) {
+    k_update_h<T, true><<<gm, 256, 0, c->stream>>>(s, y, out, c->rs, g, *next);
+  } else {
+    NextLin none{};
+    k_update_h<T, false><<<gm, 256, 0, c->stream>>>(s, y, out, c->rs, g, none);
+  }
+  prof_end(c, KK_UPDATE_H,
+           6.0 * M * sizeof(C2<T>) + (8.0 + (next ? 4.0 * (next->n + 2) : 0.0)) * g.Next * sizeof(T));
   return check_launch(c, "k_update_h");
+}
+int tensor_last_pass(Ctx *c, void *spec, void *y, void *out, const NextLin *next) {
+  if (c->mixed)
+    return tensor_last_pass_t<float>(c, (C2<float> *)spec, (float *)y, (float *)out, next);
+  return tensor_last_pass_t<double>(c, (C2<double> *)spec, (double *)y, (double *)out, next);
 }
 
 // ---------------------------------------------------------------------------
@@ -772,7 +858,8 @@ int read_output(Ctx *c, ih_output *out) {
 // ---------------------------------------------------------------------------
 // the RHS
 template <typename T>
-static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry_src) {
+static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry_src,
+                 const NextLin *next) {
   const Geom &g = c->g;
   const long long N = g.N, M = g.M;
   C2<T> *spec = (C2<T> *)c->spec[0];
@@ -830,24 +917,42 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
     // (batched: per-array y-then-x ordering measured slower, no L2 reuse)
     IH_TRY((fft_xy<T>(c, spec, M, 4, 1, -1)));
     IH_TRY((fft_xy<T>(c, spec + 5 * M, M, 2, 1, -1)));
-    IH_TRY(tensor_last_pass(c, spec, yfl, kfl));
+    IH_TRY(tensor_last_pass(c, spec, yfl, kfl, next));
   }
-  // 6. phi/psi equations of motion
+  // 6. phi/psi equations of motion (and the next stage input)
   prof_begin(c, KK_UPDATE_PHI_PSI);
-  if (c->mixed)
-    k_update_phi_psi<T, true><<<grid_for(N, 256, 4), 256, 0, c->stream>>>(
-        yfl, y.sc, lap, p, kfl, c->rs, N, g.mass);
-  else
-    k_update_phi_psi<T, false><<<grid_for(N, 256, 4), 256, 0, c->stream>>>(
-        yfl, y.sc, lap, p, kfl, c->rs, N, g.mass);
-  prof_end(c, KK_UPDATE_PHI_PSI, 10.0 * N * sizeof(T));
-  return check_launch(c, "k_update_phi_psi");
+  const NextLin none{};
+  const NextLin &nl = next ? *next : none;
+  const unsigned gu = grid_for(N / VecW<T>::W, 256, 4);
+  if (c->mixed) {
+    if (next)
+      k_update_phi_psi<T, true, true><<<gu, 256, 0, c->stream>>>(yfl, y.sc, lap, p, kfl, c->rs, N,
+                                                                 g.mass, nl);
+    else
+      k_update_phi_psi<T, true, false><<<gu, 256, 0, c->stream>>>(yfl, y.sc, lap, p, kfl, c->rs, N,
+                                                                  g.mass, nl);
+  } else {
+    if (next)
+      k_update_phi_psi<T, false, true><<<gu, 256, 0, c->stream>>>(yfl, y.sc, lap, p, kfl, c->rs,
+                                                                  N, g.mass, nl);
+    else
+      k_update_phi_psi<T, false, false><<<gu, 256, 0, c->stream>>>(yfl, y.sc, lap, p, kfl, c->rs,
+                                                                   N, g.mass, nl);
+  }
+  prof_end(c, KK_UPDATE_PHI_PSI, (10.0 + (next ? 4.0 * (next->n + 2) : 0.0)) * N * sizeof(T));
+  IH_TRY(check_launch(c, "k_update_phi_psi"));
+  if (next) {
+    k_next_sc<<<1, 32, 0, c->stream>>>(*next, k.sc, y.sc);
+    IH_TRY(check_launch(c, "k_next_sc"));
+  }
+  return IH_OK;
 }
 
-int rhs(Ctx *c, double t, Vec &y, Vec &k, int filter, int output, const Vec *smry_src) {
+int rhs(Ctx *c, double t, Vec &y, Vec &k, int filter, int output, const Vec *smry_src,
+        const NextLin *next) {
   (void)t;
-  if (c->mixed) return rhs_t<float>(c, y, k, filter, output, smry_src);
-  return rhs_t<double>(c, y, k, filter, output, smry_src);
+  if (c->mixed) return rhs_t<float>(c, y, k, filter, output, smry_src, next);
+  return rhs_t<double>(c, y, k, filter, output, smry_src, next);
 }
 
 int get_field(Ctx *c, int which, double *dev_out) {

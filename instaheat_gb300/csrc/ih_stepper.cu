@@ -126,7 +126,6 @@ void dopri_tableau(double *cc, double *a, double *b, double *bhh, double *er) {
 }
 
 // ---------------------------------------------------------------------------
-constexpr int kMaxTerms = 12;
 struct LinArgs {
   const void *in[kMaxTerms];
   const double *insc[kMaxTerms];
@@ -516,23 +515,60 @@ int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0, int want_
 // combinations and RHS evaluations, the final combination and the two error
 // sums, reduced into diag[48..50] (error(), <rho>, the NaN flag).  The step
 // size is read from c->dt_dev, so one capture serves every try.
-static int try_body(Ctx *c) {
-  for (int s = 1; s < 12; ++s) {  // stage s+1 from stages 1..s
-    LinArgs a;
-    memset(&a, 0, sizeof a);
-    int n = 0;
-    for (int j = 0; j < s; ++j) {
-      if (DA[s][j] == 0.0) continue;
-      a.in[n] = c->k[j + 1].fl;
-      a.insc[n] = c->k[j + 1].sc;
-      a.coef[n] = DA[s][j];
-      ++n;
+// The combination forming the input of iteration s of try_body (stage s+1)
+// from stages 1..s, without the term of stage s when `self` is given: that
+// term then comes from the RHS that writes stage s (NextLin).
+static void stage_terms(Ctx *c, int s, bool self, LinArgs *a, NextLin *nl) {
+  int n = 0;
+  for (int j = 0; j < (self ? s - 1 : s); ++j) {
+    if (DA[s][j] == 0.0) continue;
+    if (a) {
+      a->in[n] = c->k[j + 1].fl;
+      a->insc[n] = c->k[j + 1].sc;
+      a->coef[n] = DA[s][j];
     }
-    a.n = n;
-    a.scale_dev = c->dt_dev;
-    IH_TRY(lincomb(c, c->y, c->ytmp, a));
+    if (nl) {
+      nl->k[n] = c->k[j + 1].fl;
+      nl->ksc[n] = c->k[j + 1].sc;
+      nl->coef[n] = DA[s][j];
+      nl->coeff[n] = (float)DA[s][j];
+    }
+    ++n;
+  }
+  if (a) {
+    a->n = n;
+    a->scale_dev = c->dt_dev;
+  }
+  if (nl) {
+    nl->n = n;
+    nl->self = DA[s][s - 1];
+    nl->selff = (float)DA[s][s - 1];
+    nl->base = c->y.fl;
+    nl->basesc = c->y.sc;
+    nl->dt = c->dt_dev;
+  }
+}
+
+static int try_body(Ctx *c) {
+  // With stage fusion the RHS of stage s also forms the input of stage s+1
+  // (in ytmp, which it reads point by point before overwriting): one read
+  // of the stage vector and one launch fewer per stage.
+  // (not with the fused tensor x pass, whose variants with and without the
+  // combination do not round identically)
+  const bool fuse = c->stage_fusion && !c->tensor_fused;
+  for (int s = 1; s < 12; ++s) {  // stage s+1 from stages 1..s
+    if (s == 1 || !fuse) {  // else the previous stage's RHS formed it
+      LinArgs a;
+      memset(&a, 0, sizeof a);
+      stage_terms(c, s, false, &a, nullptr);
+      IH_TRY(lincomb(c, c->y, c->ytmp, a));
+    }
+    NextLin nl;
+    memset(&nl, 0, sizeof nl);
+    const bool fuse_next = fuse && s + 1 < 12;
+    if (fuse_next) stage_terms(c, s + 1, true, nullptr, &nl);
     // the RHS does not depend on t explicitly (toolbox.c:75-88)
-    IH_TRY(rhs(c, 0.0, c->ytmp, c->k[s + 1], 0, 0, nullptr));
+    IH_TRY(rhs(c, 0.0, c->ytmp, c->k[s + 1], 0, 0, nullptr, fuse_next ? &nl : nullptr));
   }
   FinalArgs f;
   memset(&f, 0, sizeof f);

@@ -151,45 +151,79 @@ __device__ __forceinline__ void tensor_coef(int a, int branch, T kx, T ky, T kz,
   }
 }
 
+// coefficient j of a next-stage combination in T
+template <typename T>
+__device__ __forceinline__ T nl_coef(const NextLin &nl, int j) {
+  if constexpr (sizeof(T) == 4) {
+    return nl.coeff[j];
+  } else {
+    return nl.coef[j];
+  }
+}
+template <typename T>
+__device__ __forceinline__ T nl_self(const NextLin &nl) {
+  if constexpr (sizeof(T) == 4) {
+    return nl.selff;
+  } else {
+    return nl.self;
+  }
+}
+// next-stage input at complex element e of the state (V = C2<T>): base +
+// dt (sum_j coef_j k_j + self o), written to y
+template <typename T>
+__device__ __forceinline__ void nl_apply_c(const NextLin &nl, T dt, long long e, C2<T> o,
+                                           C2<T> *y) {
+  typedef C2<T> V;
+  T ax = 0, ay = 0;
+#pragma unroll
+  for (int j = 0; j < kMaxTerms; ++j) {
+    if (j < nl.n) {
+      const V kv = reinterpret_cast<const V *>(nl.k[j])[e];
+      const T cj = nl_coef<T>(nl, j);
+      ax += cj * kv.x;
+      ay += cj * kv.y;
+    }
+  }
+  const T cs = nl_self<T>(nl);
+  ax += cs * o.x;
+  ay += cs * o.y;
+  const V bv = reinterpret_cast<const V *>(nl.base)[e];
+  y[e] = mk2c<T>(bv.x + dt * ax, bv.y + dt * ay);
+}
+
 // The equation of motion of mode id from its sources n0, n1 (zero for the
 // zero mode) and k^2: h1' = dh1, h2' = dh2,
-// dh1' = -(2 <p> + k^2/a^2) h1 - 3 H dh1 + 2/a^2 n0 (and dh2'), reading and
-// writing the tensor segments of y and out.
-template <typename T>
+// dh1' = -(2 <p> + k^2/a^2) h1 - 3 H dh1 + 2/a^2 n0 (and dh2'), reading the
+// tensor segments of y and writing those of out; NEXT: also the next stage's
+// input at the same entries of y (nl, dt = the step size in T).
+template <typename T, bool NEXT>
 __device__ __forceinline__ void tensor_eom(const Geom &g, long long id, C2<T> n0, C2<T> n1, T ksq,
-                                           const TensorConsts<T> &tc, const T *__restrict__ y,
-                                           T *__restrict__ out) {
+                                           const TensorConsts<T> &tc, T *y, T *__restrict__ out,
+                                           const NextLin &nl, T dt) {
   const long long N = g.N, Next = g.Next;
   const long long Nh1 = 4 * N, Nh2 = Nh1 + Next, Ndh1 = Nh2 + Next, Ndh2 = Ndh1 + Next;
   const T tm = -(tc.pm2 + ksq * tc.inv_a2);
   typedef C2<T> V;
-  const V *yv = reinterpret_cast<const V *>(y);
+  V *yv = reinterpret_cast<V *>(y);
   V *ov = reinterpret_cast<V *>(out);
   // the tensor segments hold complex values at 2 id (Nh1, Next are even)
-  const V h1 = yv[Nh1 / 2 + id], h2 = yv[Nh2 / 2 + id];
-  const V d1 = yv[Ndh1 / 2 + id], d2 = yv[Ndh2 / 2 + id];
-  ov[Nh1 / 2 + id] = d1;
-  ov[Nh2 / 2 + id] = d2;
-  ov[Ndh1 / 2 + id] = mk2c<T>(tm * h1.x - tc.h3 * d1.x + tc.two_inv_a2 * n0.x,
-                              tm * h1.y - tc.h3 * d1.y + tc.two_inv_a2 * n0.y);
-  ov[Ndh2 / 2 + id] = mk2c<T>(tm * h2.x - tc.h3 * d2.x + tc.two_inv_a2 * n1.x,
-                              tm * h2.y - tc.h3 * d2.y + tc.two_inv_a2 * n1.y);
-}
-
-// update_h of mode m (index id) from the six S_ij spectra v
-template <typename T>
-__device__ __forceinline__ void tensor_mode_update(const Geom &g, Mode m, long long id,
-                                                   const C2<T> (&v)[6],
-                                                   const TensorConsts<T> &tc,
-                                                   const T *__restrict__ y, T *__restrict__ out) {
-  C2<T> n0 = mk2c<T>(0, 0), n1 = mk2c<T>(0, 0);
-  T ksq = 0;
-  if (id != 0) {
-    const ModeK<T> q = mode_k<T>(g, m);
-    ksq = q.ksq;
-    tensor_sources<T>(m, q, v, n0, n1);
+  const long long e1 = Nh1 / 2 + id, e2 = Nh2 / 2 + id, e3 = Ndh1 / 2 + id, e4 = Ndh2 / 2 + id;
+  const V h1 = yv[e1], h2 = yv[e2];
+  const V d1 = yv[e3], d2 = yv[e4];
+  const V o3 = mk2c<T>(tm * h1.x - tc.h3 * d1.x + tc.two_inv_a2 * n0.x,
+                       tm * h1.y - tc.h3 * d1.y + tc.two_inv_a2 * n0.y);
+  const V o4 = mk2c<T>(tm * h2.x - tc.h3 * d2.x + tc.two_inv_a2 * n1.x,
+                       tm * h2.y - tc.h3 * d2.y + tc.two_inv_a2 * n1.y);
+  ov[e1] = d1;
+  ov[e2] = d2;
+  ov[e3] = o3;
+  ov[e4] = o4;
+  if constexpr (NEXT) {
+    nl_apply_c<T>(nl, dt, e1, d1, yv);
+    nl_apply_c<T>(nl, dt, e2, d2, yv);
+    nl_apply_c<T>(nl, dt, e3, o3, yv);
+    nl_apply_c<T>(nl, dt, e4, o4, yv);
   }
-  tensor_eom<T>(g, id, n0, n1, ksq, tc, y, out);
 }
 
 }  // namespace ih

@@ -155,6 +155,7 @@ def load(build_if_missing: bool = True):
     L.ih_fft_get_engine.argtypes = [vp, C.c_int]
     L.ih_graphs_enable.argtypes = [vp, C.c_int]
     L.ih_rhs_roundtrip.argtypes = [vp, C.c_int]
+    L.ih_stage_fusion.argtypes = [vp, C.c_int]
     L.ih_ensemble_create.argtypes = [C.POINTER(Params), C.c_int, C.POINTER(vp)]
     L.ih_ensemble_destroy.argtypes = [vp]
     L.ih_ensemble_destroy.restype = None
@@ -377,6 +378,12 @@ class Context:
         flags from x and y round trips on its z spectrum (on, the default) or
         from the full 3-D spectrum (off)."""
         self._ck(self.L_.ih_rhs_roundtrip(self.h, int(on)), "ih_rhs_roundtrip")
+
+    def stage_fusion(self, on=True):
+        """DOPRI853 stage inputs formed by the previous stage's RHS kernels
+        (on) or by separate combination passes (off, the default); the results
+        are identical to the bit."""
+        self._ck(self.L_.ih_stage_fusion(self.h, int(on)), "ih_stage_fusion")
 
     def engines(self):
         """Engines of the x, y, fused x passes, the x, y round trips, the form

@@ -380,6 +380,31 @@ def test_rhs_roundtrip_mixed_matches_full(gpu_mod, oracle_mod, n):
     assert errs["a"] < 1e-10, errs
 
 
+@pytest.mark.parametrize("prec", ["f64", "mixed"])
+@pytest.mark.parametrize("tensor_fused", [0, 1])
+def test_stage_fusion_bit_identical(gpu_mod, prec, tensor_fused):
+    """DOPRI853 with the stage inputs formed by the previous stage's RHS
+    kernels (stage fusion) or by separate combination passes: the same steps,
+    counters and states to the bit (with the fused tensor x pass the fusion
+    is not used, so the runs are the same run)."""
+    n = (32, 32, 16)
+    precision = gpu_mod.PREC_F64 if prec == "f64" else gpu_mod.PREC_MIXED
+    runs = []
+    for fuse in (False, True):
+        ctx = gpu_mod.Context(n=n, precision=precision)
+        ctx.set_engine(5, tensor_fused)
+        ctx.stage_fusion(fuse)
+        ctx.ic(seed=31, amp=1e-3)
+        ctx.dopri_init(gpu_mod.dopri_cfg(1e-8, 1e-8), 0.0, 1e-2)
+        dt = 1e-2
+        for _ in range(4):
+            dt = ctx.dopri_step(dt).dt_next
+        runs.append((ctx.get_state(), ctx.dopri_counters(), ctx.t))
+        ctx.close()
+    assert runs[0][1] == runs[1][1] and runs[0][2] == runs[1][2]
+    assert np.array_equal(runs[0][0], runs[1][0])
+
+
 def test_autotune_picks_an_engine_and_keeps_parity(gpu_mod, oracle_mod):
     n = (64, 64, 64)
     ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
