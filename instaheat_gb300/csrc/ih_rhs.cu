@@ -2,17 +2,22 @@
 // helpers on GB300: filter, pointwise equations of motion, tensor sources,
 // reductions, diagnostics, initial conditions and the psi constraint solve.
 //
-// One RHS evaluation (GW on, filter off) is this launch sequence:
-//   zr2c(phi) -> y fwd -> x fwd                       phihat          (3 FFT passes)
-//   x inv deriv4 (i k_a phihat / N, -k^2 phihat / N)   4 spectra       (fused multiply)
-//   y inv (4 arrays)
-//   z fused: 4 c2r, grad^2, rho, p, FP64 block sums, 6 products, 6 r2c(z)
+// One RHS evaluation (GW on, filter and output off) is this launch sequence:
+//   zr2c(phi) -> Z                                    z spectrum of phi
+//   x round trip(Z): d/dx Z, d2/dx2 Z                 (derivatives along one
+//   y round trip(Z): d/dy Z, laplacian                 axis commute with the
+//                                                      other axes' transforms)
+//   z fused: 4 c2r (d/dz from Z), grad^2, rho, p, FP64 block sums,
+//            6 products, 6 r2c(z)
 //   reduce_finish: <rho>, <p>, H, homogeneous RHS parts
 //   y fwd, x fwd (6 arrays)                           S_ij hat
 //   update_h: TT projection + h'' (toolbox.c:311-397)
 //   update_phi_psi (toolbox.c:282-299)
-// which is the reference's 7 r2c + 4 c2r with the spectral multiplies, the
-// pointwise products and the reductions folded into the FFT passes.
+// With the filter or output flag phihat itself is formed (zr2c, y, x), then
+// the fused inverse x pass (i k_a phihat / N, -k^2 phihat / N) and a 4-array
+// inverse y pass feed the same z pass.  Either way the reference's 7 r2c +
+// 4 c2r with the spectral multiplies, the pointwise products and the
+// reductions folded into the FFT passes.
 #include <float.h>
 #include <math.h>
 #include "ih_internal.cuh"
