@@ -208,6 +208,18 @@ def bench_form(gpu, precision, device, seed, steps, warmup, profile=False, clock
     return ctx, res
 
 
+def step_roofline(ms_per_step, peak, peak_src):
+    n = N_GRID
+    N = n ** 3
+    Next = 2 * n * n * (n // 2 + 1)
+    Ntot = 4 * N + 4 * Next + 1
+    b_step = (12 * 15 * (N + Next) + 72 * Ntot) * 4
+    achieved = b_step / (ms_per_step / 1e3) / 1e9
+    return {"bytes_per_step": b_step, "achieved": achieved, "peak": peak, "peak_source": peak_src,
+            "unit": "GB/s", "frac": achieved / peak,
+            "floor_ms_per_step": b_step / (peak * 1e9) * 1e3}
+
+
 def bench_e2e(gpu, ctx, steps):
     """Public-API loop with host buffers: upload, step, download per step."""
     Ntot = ctx.Ntot
@@ -362,6 +374,11 @@ def main():
                          "algorithmic_bytes_per_launch": dbytes / dn if dn else None,
                          "share_of_device_time": dms / total_ms if total_ms else None},
             "kernels_ms_per_step": {k: v[0] / steps for k, v in kern.items() if v[1]},
+            # the whole step against compulsory traffic: 12 RHS x 11 transforms
+            # (input read + output written once each) + the result write, and
+            # 72 state-vector passes of the stepper, B_step = [12*15*(N + Next)
+            # + 72*Ntot]*sizeof(float), over the device time of a step
+            "step_roofline": step_roofline(ms / steps, peak, peak_src),
             "cpu_baseline": cpu,
             "clocks": mixed["clocks"],
         }

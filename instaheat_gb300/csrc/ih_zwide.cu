@@ -190,26 +190,29 @@ __global__ void __launch_bounds__(32 * kWarpsW, 4) k_fft_z_rhs_wide(
 
   const long long N = g.N;
   const long long e0 = row * (2 * kH) + 4 * t;  // first real of the lane in the row
-  // 1. laplacian, written out
-  {
-    float2 v[16];
-    inverse_of(3, v);
-    if (valid) {
-#pragma unroll
-      for (int q = 0; q < 8; ++q)
-        *reinterpret_cast<float4 *>(lap + e0 + 32 * q) = f4(v[2 * q], v[2 * q + 1]);
-    }
-  }
-  // 2. d/dx, d/dy to the shared slab; 3. d/dz kept
-#pragma unroll
-  for (int a = 0; a < 2; ++a) {
+  // the four inverse transforms in one loop (one copy of the transform code:
+  // the kernel's instruction footprint): the laplacian is written out, d/dx
+  // and d/dy go to the shared slab, d/dz stays in registers
+  float2 dz[16];
+#pragma unroll 1
+  for (int i = 0; i < 4; ++i) {
+    const int a = (i + 3) & 3;  // 3, 0, 1, 2
     float2 v[16];
     inverse_of(a, v);
+    if (a == 3) {
+      if (valid) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) sm.grad[warp][a][q][lane] = f4(v[2 * q], v[2 * q + 1]);
+        for (int q = 0; q < 8; ++q)
+          *reinterpret_cast<float4 *>(lap + e0 + 32 * q) = f4(v[2 * q], v[2 * q + 1]);
+      }
+    } else if (a < 2) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) sm.grad[warp][a][q][lane] = f4(v[2 * q], v[2 * q + 1]);
+    } else {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) dz[m] = v[m];
+    }
   }
-  float2 dz[16];
-  inverse_of(2, dz);
 
   // 4. pointwise energy density and pressure, FP64 partial sums
   const double a_sc = ysc[4];
