@@ -49,14 +49,21 @@ void prof_end(Ctx *c, int kind, double bytes) {
 }
 
 static bool pow2(int n) { return n >= 1 && (n & (n - 1)) == 0; }
+// n = 2^a 3^b with a >= 1 (even: the real z transform halves nz)
+static bool smooth23(int n) {
+  if (n < 2 || n % 2) return false;
+  while (n % 2 == 0) n /= 2;
+  while (n % 3 == 0) n /= 3;
+  return n == 1;
+}
 
 static int validate(const ih_params *p, std::string *why) {
   if (!p) {
     *why = "null parameters";
     return IH_ERR_ARG;
   }
-  if (!pow2(p->nx) || !pow2(p->ny) || !pow2(p->nz)) {
-    *why = "grid sizes must be powers of two";
+  if (!smooth23(p->nx) || !smooth23(p->ny) || !smooth23(p->nz)) {
+    *why = "grid sizes must be 2^a 3^b (a >= 1): powers of two, or with a radix-3 factor";
     return IH_ERR_ARG;
   }
   if (p->nx < p->ny || p->ny < p->nz) {
@@ -123,6 +130,7 @@ static void make_geom(const ih_params *p, Geom *g) {
                                g->mz + 1);
   g->logny = 0;
   while ((1 << g->logny) < g->ny) ++g->logny;
+  g->pow2 = pow2(p->nx) && pow2(p->ny) && pow2(p->nz);
 }
 
 static int dmalloc(Ctx *c, void **p, size_t bytes) {
@@ -169,6 +177,7 @@ static int create(const ih_params *p, Ctx *c) {
   IH_TRY(dmalloc(c, &rblk, c->tsize * (size_t)g.N * 4));
   for (int i = 0; i < 4; ++i) c->rbuf[i] = (char *)rblk + c->tsize * (size_t)g.N * i;
   IH_TRY(dmalloc(c, &c->mask, c->tsize * (size_t)g.M));
+  if (!g.pow2) IH_TRY(dmalloc(c, &c->gscratch, c->tsize * (size_t)g.N * 6));
   // FP64 partial sums: the fused RHS pass writes 2 per tile of rows
   c->partials_cap = (long long)kMaxPartials * 8;
   if (2LL * g.nx * g.ny + 64 > c->partials_cap) c->partials_cap = 2LL * g.nx * g.ny + 64;
@@ -198,6 +207,7 @@ static void destroy(Ctx *c) {
   if (c->tw_z) cudaFree(c->tw_z);
   if (c->spec[0]) cudaFree(c->spec[0]);
   if (c->rbuf[0]) cudaFree(c->rbuf[0]);
+  if (c->gscratch) cudaFree(c->gscratch);
   if (c->mask) cudaFree(c->mask);
   if (c->partials) cudaFree(c->partials);
   if (c->rs) cudaFree(c->rs);

@@ -176,6 +176,76 @@ __device__ void smem_fft(C2<T> *s, int L, int P, const C2<T> *tw, int sign, int 
   }
 }
 
+// The same Stockham stages for any L = 2^a 3^b: radix 4 while 4 divides
+// the remaining length, then 2, then 3; the index arithmetic divides by the
+// stride (no longer a power of two after a radix-3 stage).  A radix-3 stage
+// is y0 = x0 + s, y1,2 = x0 - s/2 +- sign i (sqrt 3/2) d with s = x1 + x2,
+// d = x1 - x2.  Requires B*L <= 4*K*nt like smem_fft.
+template <typename T, int B, int K>
+__device__ void smem_fft_g(C2<T> *s, int L, int P, const C2<T> *tw, int sign, int tid, int nt) {
+  constexpr int LB = clog2(B);
+  constexpr int K3 = (4 * K + 2) / 3;  // radix-3 butterflies per thread
+  const T h3 = (T)0.86602540378443864676;
+  int Lc = L, st = 1;
+  while (Lc > 1) {
+    const int r = (Lc % 4 == 0) ? 4 : ((Lc % 2 == 0) ? 2 : 3);
+    const int m = Lc / r;
+    const int nb = (B * L) / r;
+    const int bpt = r == 4 ? K : (r == 2 ? 2 * K : K3);
+    C2<T> v[4 * K + 2];
+    for (int kk = 0; kk < bpt; ++kk) {
+      const int u = tid + kk * nt;
+      if (u < nb) {
+        const int b = u & (B - 1), w = u >> LB, q = w % st, pp = w / st;
+        for (int t = 0; t < r; ++t) v[kk * r + t] = s[(q + (pp + t * m) * st) * P + b];
+      }
+    }
+    __syncthreads();
+    for (int kk = 0; kk < bpt; ++kk) {
+      const int u = tid + kk * nt;
+      if (u >= nb) continue;
+      const int b = u & (B - 1), w = u >> LB, q = w % st, pp = w / st;
+      C2<T> y[4];
+      if (r == 4) {
+        const C2<T> x0 = v[kk * 4], x1 = v[kk * 4 + 1], x2 = v[kk * 4 + 2], x3 = v[kk * 4 + 3];
+        const C2<T> s02 = cadd(x0, x2), d02 = csub(x0, x2);
+        const C2<T> s13 = cadd(x1, x3), d13 = csub(x1, x3);
+        const C2<T> j13 = mk2<T>(-(T)sign * d13.y, (T)sign * d13.x);  // (sign i) d13
+        y[0] = cadd(s02, s13);
+        y[2] = csub(s02, s13);
+        y[1] = cadd(d02, j13);
+        y[3] = csub(d02, j13);
+      } else if (r == 2) {
+        const C2<T> a = v[kk * 2], c = v[kk * 2 + 1];
+        y[0] = cadd(a, c);
+        y[1] = csub(a, c);
+      } else {
+        const C2<T> x0 = v[kk * 3], x1 = v[kk * 3 + 1], x2 = v[kk * 3 + 2];
+        const C2<T> s12 = cadd(x1, x2), d12 = csub(x1, x2);
+        const C2<T> tq = mk2<T>(x0.x - (T)0.5 * s12.x, x0.y - (T)0.5 * s12.y);
+        const C2<T> jd = mk2<T>(-(T)sign * h3 * d12.y, (T)sign * h3 * d12.x);
+        y[0] = cadd(x0, s12);
+        y[1] = cadd(tq, jd);
+        y[2] = csub(tq, jd);
+      }
+      const int base = (q + r * pp * st) * P + b;
+      s[base] = y[0];
+      for (int t = 1; t < r; ++t) {
+        C2<T> yt = y[t];
+        if (pp != 0) {
+          C2<T> wt = tw[t * pp * st];
+          if (sign > 0) wt.y = -wt.y;
+          yt = cmul(yt, wt);
+        }
+        s[base + t * st * P] = yt;
+      }
+    }
+    Lc = m;
+    st *= r;
+    __syncthreads();
+  }
+}
+
 template <typename V>
 __device__ __forceinline__ V twid(const V *tw, int m, int sign) {
   V w = tw[m];
@@ -198,7 +268,9 @@ __device__ __forceinline__ void load_table(V *dst, const V *src, int n, int tid,
 //   two-step  -- L = R1 R2: each thread loads R2 elements straight into
 //                registers, runs an R2-point DFT and one twiddle, exchanges
 //                through shared memory once, runs an R1-point DFT and stores.
-template <typename T, int B>
+// GEN: L = 2^a 3^b with a radix-3 stage (a separate instantiation, so that
+// the power-of-two kernels keep their registers)
+template <typename T, int B, bool GEN = false>
 __global__ void k_fft_xy_st(C2<T> *data, long long astride, int L, long long sj,
                             long long so, int mz, int sign, const C2<T> *twg) {
   constexpr int P = B + 1;
@@ -216,7 +288,10 @@ __global__ void k_fft_xy_st(C2<T> *data, long long astride, int L, long long sj,
     s[j * P + b] = (b < bv) ? base[(long long)j * sj + b] : mk2<T>(0, 0);
   }
   __syncthreads();
-  smem_fft<T, B, kFftK>(s, L, P, tw, sign, tid, nt);
+  if constexpr (GEN)
+    smem_fft_g<T, B, kFftK>(s, L, P, tw, sign, tid, nt);
+  else
+    smem_fft<T, B, kFftK>(s, L, P, tw, sign, tid, nt);
   for (int idx = tid; idx < L * B; idx += nt) {
     const int b = idx & (B - 1), j = idx >> LB;
     if (b < bv) base[(long long)j * sj + b] = s[j * P + b];
@@ -715,7 +790,7 @@ __global__ void __launch_bounds__(32 * zwarps<T>()) k_fft_zc2r(const C2<T> *in, 
 // Two engines, as for the plain passes: Stockham (the phihat tile stays in
 // shared memory for the four variants) and two-step (each step-1 thread keeps
 // its R2 values of phihat in registers for the four variants).
-template <typename T, int B>
+template <typename T, int B, bool GEN = false>
 __global__ void k_fft_x_deriv4_st(const C2<T> *phihat, C2<T> *out, long long ostride, Geom g,
                                    const C2<T> *twg) {
   constexpr int P = B + 1;
@@ -763,7 +838,10 @@ __global__ void k_fft_x_deriv4_st(const C2<T> *phihat, C2<T> *out, long long ost
                              : mk2<T>(-pre.x * f, -pre.y * f);  // -pre * k^2
     }
     __syncthreads();
-    smem_fft<T, B, kFftK>(s, L, P, tw, +1, tid, nt);
+    if constexpr (GEN)
+      smem_fft_g<T, B, kFftK>(s, L, P, tw, +1, tid, nt);
+    else
+      smem_fft<T, B, kFftK>(s, L, P, tw, +1, tid, nt);
     C2<T> *o = out + a * ostride + off;
     for (int idx = tid; idx < L * B; idx += nt) {
       const int b = idx & (B - 1), j = idx >> LB;
@@ -946,6 +1024,92 @@ __global__ void __launch_bounds__(pass_threads<L, B>(), 2) k_fft_x_deriv4_pipe(c
     __syncthreads();  // bc is the prefetch target of the next iteration
   }
   cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
+// z passes for any H = nz/2 = 2^a 3^b (the warp engine above needs powers of
+// two): a CTA stages kZB rows in shared memory [H][kZB+1] (element j of row
+// b), runs the Stockham stages along the rows and does the even/odd split of
+// the real transform there (the same split as the warp engine).
+constexpr int kZB = 16;
+template <typename T> constexpr size_t zg_smem(int H) {
+  return sizeof(C2<T>) * ((size_t)H + 2 * (size_t)H + (size_t)H * (kZB + 1));
+}
+
+template <typename T>
+__global__ void k_fft_zr2c_g(const T *in, long long istride, C2<T> *out, long long ostride,
+                             long long rows, int H, const C2<T> *twhg, const C2<T> *twzg) {
+  constexpr int P = kZB + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<T> *twh = reinterpret_cast<C2<T> *>(smraw);  // exp(-2 pi i k/H)
+  C2<T> *twz = twh + H;                           // exp(-2 pi i k/nz)
+  C2<T> *s = twz + 2 * H;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  load_table(twh, twhg, H, tid, nt);
+  load_table(twz, twzg, 2 * H, tid, nt);
+  const long long r0 = (long long)blockIdx.x * kZB;
+  const T *src = in + blockIdx.y * istride;
+  C2<T> *dst = out + blockIdx.y * ostride;
+  for (int idx = tid; idx < H * kZB; idx += nt) {  // row b, complex j = reals 2j, 2j+1
+    const int j = idx % H, b = idx / H;
+    const long long r = r0 + b;
+    s[j * P + b] = (r < rows) ? *reinterpret_cast<const C2<T> *>(src + r * 2 * H + 2 * j)
+                              : mk2<T>(0, 0);
+  }
+  __syncthreads();
+  smem_fft_g<T, kZB, kFftK>(s, H, P, twh, -1, tid, nt);
+  // X_k = E_k + exp(-2 pi i k/nz) O_k, E = (Z_k + conj Z_(H-k))/2,
+  // O = (Z_k - conj Z_(H-k))/(2i), k = 0..H (Z_H = Z_0)
+  for (int idx = tid; idx < (H + 1) * kZB; idx += nt) {
+    const int k = idx % (H + 1), b = idx / (H + 1);
+    const long long r = r0 + b;
+    if (r >= rows) continue;
+    const C2<T> z = s[(k % H) * P + b], zp = s[((H - k) % H) * P + b];
+    const C2<T> zc = mk2<T>(zp.x, -zp.y);
+    const C2<T> e = mk2<T>((T)0.5 * (z.x + zc.x), (T)0.5 * (z.y + zc.y));
+    const C2<T> o = mk2<T>((T)0.5 * (z.y - zc.y), -(T)0.5 * (z.x - zc.x));
+    dst[r * (H + 1) + k] = cadd(e, cmul(o, twz[k]));
+  }
+}
+
+template <typename T>
+__global__ void k_fft_zc2r_g(const C2<T> *in, long long istride, T *out, long long ostride,
+                             long long rows, int H, const C2<T> *twhg, const C2<T> *twzg) {
+  constexpr int P = kZB + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<T> *twh = reinterpret_cast<C2<T> *>(smraw);
+  C2<T> *twz = twh + H;
+  C2<T> *s = twz + 2 * H;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  load_table(twh, twhg, H, tid, nt);
+  load_table(twz, twzg, 2 * H, tid, nt);
+  __syncthreads();
+  const long long r0 = (long long)blockIdx.x * kZB;
+  const C2<T> *src = in + blockIdx.y * istride;
+  T *dst = out + blockIdx.y * ostride;
+  // Z_k = E + i O, E = X_k + conj X_(H-k), O = (X_k - conj X_(H-k)) exp(+2 pi i k/nz)
+  for (int idx = tid; idx < H * kZB; idx += nt) {
+    const int k = idx % H, b = idx / H;
+    const long long r = r0 + b;
+    C2<T> zv = mk2<T>(0, 0);
+    if (r < rows) {
+      const C2<T> x = src[r * (H + 1) + k], xp = src[r * (H + 1) + (H - k)];
+      const C2<T> pc = mk2<T>(xp.x, -xp.y);
+      const C2<T> e = cadd(x, pc), d = csub(x, pc);
+      C2<T> wn = twz[k];
+      wn.y = -wn.y;
+      const C2<T> o = cmul(d, wn);
+      zv = mk2<T>(e.x - o.y, e.y + o.x);
+    }
+    s[k * P + b] = zv;
+  }
+  __syncthreads();
+  smem_fft_g<T, kZB, kFftK>(s, H, P, twh, +1, tid, nt);
+  for (int idx = tid; idx < H * kZB; idx += nt) {  // z_j = reals 2j, 2j+1
+    const int j = idx % H, b = idx / H;
+    const long long r = r0 + b;
+    if (r < rows) *reinterpret_cast<C2<T> *>(dst + r * 2 * H + 2 * j) = s[j * P + b];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1415,12 +1579,13 @@ struct XYLaunch {
   C2<T> *data;
   long long stride;
   int count, axis, sign, var;
-  template <int B>
+  template <int B, bool GEN = false>
   int run_st(int L, dim3 grid, long long sj, long long so, const C2<T> *tw) {
     const size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * (B + 1));
-    cudaFuncSetAttribute(k_fft_xy_st<T, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_fft_xy_st<T, B><<<grid, threads_st(L, B), sm, c->stream>>>(data, stride, L, sj, so, c->g.mz,
-                                                                  sign, tw);
+    cudaFuncSetAttribute(k_fft_xy_st<T, B, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm);
+    k_fft_xy_st<T, B, GEN><<<grid, threads_st(L, B), sm, c->stream>>>(data, stride, L, sj, so,
+                                                                       c->g.mz, sign, tw);
     return IH_OK;
   }
   template <int L, int B>
@@ -1493,8 +1658,18 @@ int fft_xy(Ctx *c, C2<T> *data, long long stride, int count, int axis, int sign)
   const Geom &g = c->g;
   const int L = axis == 0 ? g.nx : g.ny;
   prof_begin(c, KK_FFT_XY);
-  IH_TRY(dispatch_len(L, XYLaunch<T>{c, data, stride, count, axis, sign, c->xy_var[axis]},
-                      allow512<T>()));
+  if (L & (L - 1)) {  // 2^a 3^b: the Stockham engine with a radix-3 stage
+    constexpr int B = tileB<T>();
+    const long long sj = axis == 0 ? (long long)g.ny * g.mz : g.mz;
+    const long long so = axis == 0 ? g.mz : (long long)g.ny * g.mz;
+    const int outer = axis == 0 ? g.ny : g.nx;
+    XYLaunch<T> xl{c, data, stride, count, axis, sign, FV_STOCKHAM};
+    IH_TRY((xl.template run_st<B, true>(L, dim3((g.mz + B - 1) / B, outer, count), sj, so,
+                                        tab<T>(axis == 0 ? c->tw_x : c->tw_y))));
+  } else {
+    IH_TRY(dispatch_len(L, XYLaunch<T>{c, data, stride, count, axis, sign, c->xy_var[axis]},
+                        allow512<T>()));
+  }
   prof_end(c, KK_FFT_XY, 2.0 * count * g.M * sizeof(C2<T>));
   return check_launch(c, "k_fft_xy");
 }
@@ -1537,7 +1712,16 @@ int fft_zr2c(Ctx *c, const T *in, long long in_stride, C2<T> *out, long long out
              int count) {
   const Geom &g = c->g;
   prof_begin(c, KK_FFT_ZR2C);
-  IH_TRY(dispatch_len(g.h, ZLaunch<T>{c, in, in_stride, out, out_stride, count, true}, false));
+  if (g.h & (g.h - 1)) {
+    const long long rows = (long long)g.nx * g.ny;
+    const size_t sm = zg_smem<T>(g.h);
+    cudaFuncSetAttribute(k_fft_zr2c_g<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_fft_zr2c_g<T><<<dim3((unsigned)((rows + kZB - 1) / kZB), count), threads_st(g.h, kZB), sm,
+                      c->stream>>>(in, in_stride, out, out_stride, rows, g.h, tab<T>(c->tw_h),
+                                   tab<T>(c->tw_z));
+  } else {
+    IH_TRY(dispatch_len(g.h, ZLaunch<T>{c, in, in_stride, out, out_stride, count, true}, false));
+  }
   prof_end(c, KK_FFT_ZR2C, (double)count * (g.N * sizeof(T) + g.M * sizeof(C2<T>)));
   return check_launch(c, "k_fft_zr2c");
 }
@@ -1547,7 +1731,16 @@ int fft_zc2r(Ctx *c, const C2<T> *in, long long in_stride, T *out, long long out
              int count) {
   const Geom &g = c->g;
   prof_begin(c, KK_FFT_ZC2R);
-  IH_TRY(dispatch_len(g.h, ZLaunch<T>{c, in, in_stride, out, out_stride, count, false}, false));
+  if (g.h & (g.h - 1)) {
+    const long long rows = (long long)g.nx * g.ny;
+    const size_t sm = zg_smem<T>(g.h);
+    cudaFuncSetAttribute(k_fft_zc2r_g<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_fft_zc2r_g<T><<<dim3((unsigned)((rows + kZB - 1) / kZB), count), threads_st(g.h, kZB), sm,
+                      c->stream>>>(in, in_stride, out, out_stride, rows, g.h, tab<T>(c->tw_h),
+                                   tab<T>(c->tw_z));
+  } else {
+    IH_TRY(dispatch_len(g.h, ZLaunch<T>{c, in, in_stride, out, out_stride, count, false}, false));
+  }
   prof_end(c, KK_FFT_ZC2R, (double)count * (g.N * sizeof(T) + g.M * sizeof(C2<T>)));
   return check_launch(c, "k_fft_zc2r");
 }
@@ -1609,6 +1802,19 @@ struct D4Launch {
                                                             tab<T>(c->tw_x));
     return IH_OK;
   }
+  // the Stockham form (GEN: the only form for L = 2^a 3^b with b > 0)
+  template <bool GEN = false>
+  int run_st(int L) {
+    constexpr int B = tileB<T>();
+    const Geom &g = c->g;
+    dim3 grid((g.mz + B - 1) / B, g.ny, 1);
+    const size_t sm = sizeof(C2<T>) * ((size_t)L + 2 * (size_t)L * (B + 1));
+    cudaFuncSetAttribute(k_fft_x_deriv4_st<T, B, GEN>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_fft_x_deriv4_st<T, B, GEN><<<grid, threads_st(L, B), sm, c->stream>>>(
+        phihat, out, out_stride, g, tab<T>(c->tw_x));
+    return IH_OK;
+  }
   template <int L>
   int run() {
     if constexpr (L == 512 && !allow512<T>()) {
@@ -1618,14 +1824,7 @@ struct D4Launch {
       if (var == FV_PIPELINED) return run_pipe<L, B>();
       if (var == FV_TWOSTEP) return run_2s<L, B>();
       if (var == FV_TWOSTEP_HALF) return run_2s<L, B / 2>();
-      const Geom &g = c->g;
-      dim3 grid((g.mz + B - 1) / B, g.ny, 1);
-      const size_t sm = sizeof(C2<T>) * ((size_t)L + 2 * (size_t)L * (B + 1));
-      cudaFuncSetAttribute(k_fft_x_deriv4_st<T, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)sm);
-      k_fft_x_deriv4_st<T, B><<<grid, threads_st(L, B), sm, c->stream>>>(phihat, out, out_stride,
-                                                                          g, tab<T>(c->tw_x));
-      return IH_OK;
+      return run_st(L);
     }
   }
 };
@@ -1634,7 +1833,10 @@ template <typename T>
 int fft_x_deriv4_inv(Ctx *c, const C2<T> *phihat, C2<T> *out, long long out_stride) {
   const Geom &g = c->g;
   prof_begin(c, KK_X_DERIV4);
-  IH_TRY(dispatch_len(g.nx, D4Launch<T>{c, phihat, out, out_stride, c->d4_var}, allow512<T>()));
+  if (g.nx & (g.nx - 1))
+    IH_TRY((D4Launch<T>{c, phihat, out, out_stride, FV_STOCKHAM}.template run_st<true>(g.nx)));
+  else
+    IH_TRY(dispatch_len(g.nx, D4Launch<T>{c, phihat, out, out_stride, c->d4_var}, allow512<T>()));
   prof_end(c, KK_X_DERIV4, 5.0 * g.M * sizeof(C2<T>));
   return check_launch(c, "k_fft_x_deriv4_inv");
 }
@@ -1854,6 +2056,14 @@ template <typename T>
 static int autotune_t(Ctx *c) {
   const Geom &g = c->g;
   const long long M = g.M;
+  if (!g.pow2) {  // 2^a 3^b: one engine per pass
+    c->xy_var[0] = c->xy_var[1] = c->d4_var = FV_STOCKHAM;
+    c->tensor_fused = 0;
+    c->tune_report =
+        "grid with a radix-3 factor: Stockham x/y passes, shared-memory z passes, the "
+        "full-spectrum RHS route";
+    return IH_OK;
+  }
   C2<T> *sp = reinterpret_cast<C2<T> *>(c->spec[0]);
   IH_CUDA(c, cudaMemsetAsync(sp, 0, sizeof(C2<T>) * 7 * (size_t)M, c->stream));
   cudaEvent_t e0, e1;

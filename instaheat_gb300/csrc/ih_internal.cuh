@@ -54,6 +54,7 @@ struct Geom {
   // (division by an invariant integer, Granlund-Montgomery); ny = 1 << logny
   unsigned mz_magic;
   int mz_shift, logny;
+  int pow2;                     // every axis a power of two (else 2^a 3^b: the generic route)
 };
 
 // RHS scalars produced on the device by the reduction-finish kernel.
@@ -145,6 +146,7 @@ struct Ctx {
   // RHS temporaries
   void *spec[7] = {};           // complex M each (T)
   void *rbuf[4] = {};           // real N each: 0 lap, 1 p (fluct), 2 rho (fluct), 3 lap psi
+  void *gscratch = nullptr;     // real 6N: derivative fields / GW products of the generic route
   void *mask = nullptr;         // filter mask, M values of T
   double *partials = nullptr;   // partials_cap doubles
   long long partials_cap = 0;

@@ -22,6 +22,7 @@
 #include <math.h>
 #include "ih_internal.cuh"
 #include "ih_tensor.cuh"
+#include "ih_fftcore.cuh"
 
 namespace ih {
 
@@ -324,8 +325,13 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (NEXT ? 3 : 5) : 2)) k_
     const unsigned r = (__umulhi(uid, mz_magic) + uid) >> mz_shift;
     Mode m;
     m.k = (int)(uid - r * (unsigned)g.mz);
-    m.j = (int)(r & (unsigned)(g.ny - 1));
-    m.i = (int)(r >> logny);
+    if (g.pow2) {
+      m.j = (int)(r & (unsigned)(g.ny - 1));
+      m.i = (int)(r >> logny);
+    } else {
+      m.j = (int)(r % (unsigned)g.ny);
+      m.i = (int)(r / (unsigned)g.ny);
+    }
     C2<T> n0 = mk2c<T>(0, 0), n1 = mk2c<T>(0, 0);
     T ksq = 0;
     if (id != 0) {  // the zero mode has no sources (its spectra are not read)
@@ -348,7 +354,7 @@ template <typename T>
 static int tensor_last_pass_t(Ctx *c, C2<T> *s, T *y, T *out, const NextLin *next) {
   const Geom &g = c->g;
   const long long M = g.M;
-  if (c->tensor_fused) return fft_x_tensor<T>(c, s, s + 5 * M, y, out, next);
+  if (c->tensor_fused && g.pow2) return fft_x_tensor<T>(c, s, s + 5 * M, y, out, next);
   IH_TRY((fft_xy<T>(c, s, M, 4, 0, -1)));
   IH_TRY((fft_xy<T>(c, s + 5 * M, M, 2, 0, -1)));
   const unsigned gm = grid_for(M, 256, 4);
@@ -861,6 +867,80 @@ int read_output(Ctx *c, ih_output *out) {
 }
 
 // ---------------------------------------------------------------------------
+// The z part of the RHS for grids with a radix-3 factor, unfused: 4 c2r
+// passes (d/dx, d/dy, d/dz into the scratch, the laplacian into lap), one
+// pointwise pass (rho, p, their FP64 block sums, the six GW products d_i phi
+// d_j phi written over the derivatives and into the rest of the scratch) and
+// 6 r2c passes -- the same quantities as the fused pass (toolbox.c:129-250,
+// 410-424).
+template <typename T, bool MIXED>
+__global__ void k_pointwise_g(const T *__restrict__ yfl, const double *ysc, T *g0, T *g1, T *g2,
+                              T *g3, T *g4, T *g5, T *pout, T *rhoout, int gw, long long N,
+                              double mass, double *partials) {
+  const double a_sc = ysc[4];
+  const T inv_a2 = (T)(1.0 / (a_sc * a_sc));
+  const T m2 = (T)(mass * mass);
+  const T third = (T)(1.0 / 3.0);
+  const T phib = (T)ysc[0], pib = (T)ysc[1], psib = (T)ysc[2];
+  double sr = 0.0, sp = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x) {
+    const T dx = g0[i], dy = g1[i], dz = g2[i];
+    T rho, p;
+    rho_p<T, MIXED>(dx, dy, dz, yfl[i], yfl[N + i], yfl[2 * N + i], inv_a2, m2, third, phib, pib,
+                    psib, rho, p);
+    pout[i] = p;
+    if (rhoout) rhoout[i] = rho;
+    sr += (double)rho;
+    sp += (double)p;
+    if (gw) {
+      g0[i] = dx * dx;
+      g1[i] = dx * dy;
+      g2[i] = dx * dz;
+      g3[i] = dy * dy;
+      g4[i] = dy * dz;
+      g5[i] = dz * dz;
+    }
+  }
+  sr = block_sum(sr);
+  sp = block_sum(sp);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = sr;
+    partials[2 * blockIdx.x + 1] = sp;
+  }
+}
+
+template <typename T>
+static int z_pass_generic(Ctx *c, C2<T> *spec, const T *yfl, const double *ysc, T *lap, T *p,
+                          T *rho, int *nblk_out) {
+  const Geom &g = c->g;
+  const long long N = g.N, M = g.M;
+  T *gs = (T *)c->gscratch;
+  const int gw = c->p.enable_gw;
+  IH_TRY((fft_zc2r<T>(c, spec, M, gs, N, 3)));
+  IH_TRY((fft_zc2r<T>(c, spec + 3 * M, M, lap, N, 1)));
+  unsigned nb = grid_for(N, 256, 4);
+  if (2LL * nb > c->partials_cap) nb = (unsigned)(c->partials_cap / 2);
+  prof_begin(c, KK_Z_RHS_FUSED);
+  if (c->mixed)
+    k_pointwise_g<T, true><<<nb, 256, 0, c->stream>>>(yfl, ysc, gs, gs + N, gs + 2 * N, gs + 3 * N,
+                                                      gs + 4 * N, gs + 5 * N, p, rho, gw, N,
+                                                      g.mass, c->partials);
+  else
+    k_pointwise_g<T, false><<<nb, 256, 0, c->stream>>>(yfl, ysc, gs, gs + N, gs + 2 * N,
+                                                       gs + 3 * N, gs + 4 * N, gs + 5 * N, p, rho,
+                                                       gw, N, g.mass, c->partials);
+  prof_end(c, KK_Z_RHS_FUSED, (6.0 + (gw ? 6.0 : 0.0) + (rho ? 1.0 : 0.0)) * N * sizeof(T));
+  IH_TRY(check_launch(c, "k_pointwise_g"));
+  *nblk_out = (int)nb;
+  if (gw) {  // xx, xy, xz, yy -> spec[0..3]; yz, zz -> spec[5], spec[6]
+    IH_TRY((fft_zr2c<T>(c, gs, N, spec, M, 4)));
+    IH_TRY((fft_zr2c<T>(c, gs + 4 * N, N, spec + 5 * M, M, 2)));
+  }
+  return IH_OK;
+}
+
+// ---------------------------------------------------------------------------
 // the RHS
 template <typename T>
 static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry_src,
@@ -877,7 +957,7 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
   // without the filter and the output flag nothing needs the full spectrum
   // of phi: the derivatives come from round trips along x and y on its z
   // spectrum Z (spec[4]), the z parts from Z inside the fused z pass
-  const int use_rt = c->roundtrip && !do_filter && output != 1;
+  const int use_rt = c->roundtrip && c->g.pow2 && !do_filter && output != 1;
   const unsigned gm = grid_for(M, 256, 4);
   // 1. phihat (and with the filter: dphi, psi, dpsi spectra, mask, write back)
   if (do_filter) {
@@ -910,8 +990,11 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
   }
   // 3. fused inverse z + pointwise + GW products forward z
   int nblk = 0;
-  IH_TRY((fft_z_rhs_fused<T>(c, spec, yfl, y.sc, lap, p, output == 1 ? rho : nullptr, spec,
-                             c->p.enable_gw, c->partials, &nblk, use_rt)));
+  if (c->g.pow2)
+    IH_TRY((fft_z_rhs_fused<T>(c, spec, yfl, y.sc, lap, p, output == 1 ? rho : nullptr, spec,
+                               c->p.enable_gw, c->partials, &nblk, use_rt)));
+  else
+    IH_TRY((z_pass_generic<T>(c, spec, yfl, y.sc, lap, p, output == 1 ? rho : nullptr, &nblk)));
   k_reduce_finish<<<1, 256, 0, c->stream>>>(c->partials, nblk, g, y.sc, k.sc, c->rs, c->mixed);
   IH_TRY(check_launch(c, "k_reduce_finish"));
   // 4. diagnostics that need <rho> and H

@@ -38,12 +38,16 @@ __device__ __forceinline__ double kzf_of(const Geom &g, int k) { return g.kzu * 
 __device__ __forceinline__ double kz_deriv(const Geom &g, int k) {
   return (2 * k == g.nz) ? 0.0 : g.kzu * k;
 }
+// |k|^2 with the reference's operations in its order and no fused
+// multiply-adds (setup.c:609-666, compiled without contraction): the same
+// roundings as the C code, so that modes on a shell boundary of the spectra
+// (bins |k| / k_max an integer, e.g. the grid corners) fall into the same bin
 __device__ __forceinline__ double ksq64(const Geom &g, int i, int j, int k) {
-  double q = g.kz2 * k * k;
-  int ia = (i > g.nx / 2) ? (g.nx - i) : i;
-  int ja = (j > g.ny / 2) ? (g.ny - j) : j;
-  q += g.kx2 * ia * ia;
-  q += g.ky2 * ja * ja;
+  const int ia = (i > g.nx / 2) ? (g.nx - i) : i;
+  const int ja = (j > g.ny / 2) ? (g.ny - j) : j;
+  double q = __dmul_rn(__dmul_rn(g.kz2, (double)k), (double)k);
+  q = __dadd_rn(q, __dmul_rn(__dmul_rn(g.kx2, (double)ia), (double)ia));
+  q = __dadd_rn(q, __dmul_rn(__dmul_rn(g.ky2, (double)ja), (double)ja));
   return q;
 }
 

@@ -47,7 +47,8 @@ def test_invalid_grid_is_rejected_before_any_device_call(gpu_mod):
     import ctypes as C
     L = gpu_mod.load()
     h = C.c_void_p()
-    bad = [(24, 24, 24), (16, 32, 16), (16, 16, 4), (1024, 64, 64)]
+    # a prime factor other than 2 and 3, odd, out of order, too small, too large
+    bad = [(20, 20, 20), (28, 28, 14), (27, 27, 27), (16, 32, 16), (16, 16, 4), (1024, 64, 64)]
     for n in bad:
         p = gpu_mod.Params(n[0], n[1], n[2], 20.0, 20.0, 20.0, 1.0, 1, 1, 8, 0, 0)
         assert L.ih_create(C.byref(p), C.byref(h)) == 1  # IH_ERR_ARG

@@ -50,3 +50,27 @@ def test_ensemble_autotune_shares_engines(gpu_mod):
     ens.autotune()
     assert ens.members[0].engines() == ens.members[2].engines()
     ens.close()
+
+
+def test_ensemble_with_radix3_members(gpu_mod):
+    """Members of 24^3, 48^3 and 96^3 (the radix-3 sizes of the mixed-size
+    ensembles) stepped together follow the single runs exactly."""
+    members = [dict(n=(24, 24, 24), L=(20.0, 20.0, 20.0), precision=1),
+               dict(n=(48, 48, 48), L=(30.0, 30.0, 30.0), precision=1),
+               dict(n=(96, 96, 96), L=(40.0, 40.0, 40.0), precision=1),
+               dict(n=(32, 32, 32), L=(10.0, 10.0, 10.0), precision=0)]
+    tf = 0.05
+    cfg = gpu_mod.dopri_cfg(1e-8, 1e-8)
+    ens = gpu_mod.Ensemble(members)
+    for i, m in enumerate(ens.members):
+        m.ic(seed=200 + i, phi0=1.0 + 0.05 * i, amp=1e-3)
+    ens.dopri_init(cfg, 0.0, 2e-3)
+    ens.run(tf)
+    for i, m in enumerate(members):
+        ctx = gpu_mod.Context(n=m["n"], L=m["L"], precision=m["precision"])
+        ctx.ic(seed=200 + i, phi0=1.0 + 0.05 * i, amp=1e-3)
+        ctx.dopri_init(cfg, 0.0, 2e-3)
+        ctx.dopri_run(tf)
+        assert np.array_equal(ens.members[i].get_state(), ctx.get_state()), i
+        ctx.close()
+    ens.close()

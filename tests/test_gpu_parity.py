@@ -473,3 +473,85 @@ def test_graph_replay_is_identical_to_direct_launches(gpu_mod, oracle_mod, prec)
     assert q1 == q2
     assert np.array_equal(s1, s2)
     assert c1 == c2 and l1 == l2
+
+
+# grids with a radix-3 factor (2^a 3^b): Stockham x/y passes with a radix-3
+# stage, shared-memory z passes, the unfused z part of the RHS
+RADIX3 = [((24, 24, 24), (20.0, 20.0, 20.0)), ((48, 24, 12), (20.0, 15.0, 12.0)),
+          ((36, 18, 12), (18.0, 12.0, 10.0)), ((96, 96, 96), (20.0, 20.0, 20.0))]
+
+
+@pytest.mark.parametrize("n,L", RADIX3)
+def test_fft_radix3_f64(gpu_mod, oracle_mod, n, L):
+    """FFTs of 2^a 3^b grids within 1e-13 of the oracle (FP64)."""
+    ctx = gpu_mod.Context(n=n, L=L, precision=gpu_mod.PREC_F64)
+    o = oracle_mod.Oracle(n=n, L=L)
+    x = np.random.default_rng(5).standard_normal(n)
+    R = o.fft(x)
+    assert np.abs(ctx.fft(x) - R).max() <= 1e-13 * np.abs(R).max()
+    yr = o.ifft(R)
+    assert np.abs(ctx.ifft(R) - yr).max() <= 1e-13 * np.abs(yr).max()
+
+
+@pytest.mark.parametrize("n,L", RADIX3)
+@pytest.mark.parametrize("filt,out", [(0, 0), (1, 0), (1, 1)])
+def test_rhs_radix3_f64_parity(gpu_mod, oracle_mod, n, L, filt, out):
+    """The RHS on 2^a 3^b grids (FP64) within 1e-11 of the oracle, every
+    segment; with the output flag the spectra and summaries as for powers of
+    two."""
+    ctx = gpu_mod.Context(n=n, L=L, precision=gpu_mod.PREC_F64)
+    o = oracle_mod.Oracle(n=n, L=L)
+    f = make_state(o, seed=27)
+    d = oracle_mod.DiagOutput(o.bins)
+    r_ref, f_ref = o.rhs(f, filter=filt, output=out, diag=d)
+    r_gpu, f_gpu = ctx.mk_rhs(f, filter=filt, output=out)
+    errs = seg_rel_err(r_gpu, r_ref, o.N, o.Next)
+    assert max(errs.values()) < 1e-11, errs
+    assert np.abs(f_gpu - f_ref).max() < 1e-13
+    if out:
+        g = ctx.output()
+        for k in ("phi_ps", "psi_ps", "rho_ps", "gw"):
+            ref = getattr(d, k)
+            assert np.abs(g[k] - ref).max() <= 1e-10 * np.abs(ref).max(), k
+        np.testing.assert_allclose(g["smry"], d.smry, rtol=1e-9, atol=1e-14)
+
+
+def test_rhs_radix3_mixed(gpu_mod, oracle_mod):
+    """Mixed form on 96^3: fluctuation parts within 1e-5, a' within 1e-10."""
+    n = (96, 96, 96)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=28)
+    r_ref, _ = o.rhs(f)
+    r_gpu, _ = ctx.mk_rhs(f)
+    N = o.N
+    for s in range(4):
+        ref = r_ref[s * N:(s + 1) * N]
+        got = r_gpu[s * N:(s + 1) * N]
+        fl = np.abs((got - got.mean()) - (ref - ref.mean())).max()
+        assert fl <= 1e-5 * np.abs(ref - ref.mean()).max(), s
+    errs = seg_rel_err(r_gpu, r_ref, o.N, o.Next)
+    assert max(errs[k] for k in ("h1", "h2", "dh1", "dh2")) < 1e-4, errs
+    assert errs["a"] < 1e-10, errs
+
+
+def test_dopri853_radix3_steps_parity(gpu_mod, oracle_mod):
+    """Three DOPRI853 steps on 24^3 (FP64): step sizes and states as the oracle."""
+    n = (24, 24, 24)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=29)
+    cfg_o = oracle_mod.default_cfg(1e-10, 1e-10, 1e-2)
+    cfg_g = gpu_mod.dopri_cfg(1e-10, 1e-10, max_dt_hubble_fraction=1e-2)
+    ctx.set_state(f)
+    ctx.dopri_init(cfg_g, 0.0, 1e-2)
+    fo = f.copy()
+    st, dfo = o.dopri_init(fo, cfg_o, 0.0, 1e-2)
+    dt_g = dt_o = 1e-2
+    for _ in range(3):
+        info = ctx.dopri_step(dt_g)
+        o.dopri_step(fo, dfo, cfg_o, st, dt_o)
+        assert abs(info.dt_did - st.dt_did) <= 1e-12 * st.dt_did
+        dt_g, dt_o = info.dt_next, st.dt_next
+    errs = seg_rel_err(ctx.get_state(), fo, o.N, o.Next)
+    assert max(errs.values()) < 1e-11, errs
