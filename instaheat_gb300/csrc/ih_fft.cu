@@ -1272,7 +1272,7 @@ template <typename T> constexpr size_t xt_smem(int L, int B) {
 template <typename T, int L, int B, bool NEXT>
 __global__ void __launch_bounds__(L / 4 * B, (xt_min_blocks<T, L, B>())) k_fft_x_tensor(
     const C2<T> *s03, const C2<T> *s45, long long astride, T *y, T *__restrict__ out,
-    const RhsScalars *rs, Geom g, const C2<T> *twg, const NextLin nl) {
+    const RhsScalars *rs, Geom g, const C2<T> *twg, const NextLin nl, double *outsc) {
   constexpr int Q = L / 4, LB = clog2(B);
   constexpr bool R2F = (clog2(L) & 1) != 0;
   constexpr int NS0 = R2F ? 2 : 4;                                   // span after the first stage
@@ -1369,6 +1369,7 @@ __global__ void __launch_bounds__(L / 4 * B, (xt_min_blocks<T, L, B>())) k_fft_x
       n1[r] = mk2<T>(n1[r].x + be * v[r].x, n1[r].y + be * v[r].y);
     }
   }
+  T mx = 0;
   if (b < bv) {
     const TensorConsts<T> tc(rs);
     const T dt = NEXT ? (T)*nl.dt : (T)0;
@@ -1378,10 +1379,11 @@ __global__ void __launch_bounds__(L / 4 * B, (xt_min_blocks<T, L, B>())) k_fft_x
       const long long id = (long long)m.i * sj + off + b;
       const T ksq = mode_k<T>(g, m).ksq;
       const C2<T> zero = mk2<T>(0, 0);
-      tensor_eom<T, NEXT>(g, id, id != 0 ? n0[r] : zero, id != 0 ? n1[r] : zero,
-                          id != 0 ? ksq : (T)0, tc, y, out, nl, dt);
+      mx = fmax(mx, tensor_eom<T, NEXT>(g, id, id != 0 ? n0[r] : zero, id != 0 ? n1[r] : zero,
+                                        id != 0 ? ksq : (T)0, tc, y, out, nl, dt));
     }
   }
+  dh_max_store<T>(mx, outsc);
 }
 
 
@@ -1893,6 +1895,7 @@ struct XTLaunch {
   const C2<T> *s03, *s45;
   T *y;
   T *out;
+  double *outsc;
   const NextLin *next;
   template <int L, bool NEXT>
   void go() {
@@ -1904,7 +1907,7 @@ struct XTLaunch {
     const NextLin nl = next ? *next : NextLin{};
     k_fft_x_tensor<T, L, B, NEXT><<<dim3((g.mz + B - 1) / B, g.ny, 1), L / 4 * B, sm,
                                      c->stream>>>(s03, s45, g.M, y, out, c->rs, g,
-                                                  tab<T>(c->tw_x), nl);
+                                                  tab<T>(c->tw_x), nl, outsc);
   }
   template <int L>
   int run() {
@@ -1921,11 +1924,11 @@ struct XTLaunch {
 };
 
 template <typename T>
-int fft_x_tensor(Ctx *c, const C2<T> *s03, const C2<T> *s45, T *y, T *out,
+int fft_x_tensor(Ctx *c, const C2<T> *s03, const C2<T> *s45, T *y, T *out, double *outsc,
                  const NextLin *next) {
   const Geom &g = c->g;
   prof_begin(c, KK_X_TENSOR);
-  IH_TRY(dispatch_len(g.nx, XTLaunch<T>{c, s03, s45, y, out, next}, allow512<T>()));
+  IH_TRY(dispatch_len(g.nx, XTLaunch<T>{c, s03, s45, y, out, outsc, next}, allow512<T>()));
   prof_end(c, KK_X_TENSOR,
            6.0 * g.M * sizeof(C2<T>) + (8.0 + (next ? 4.0 * (next->n + 2) : 0.0)) * g.Next * sizeof(T));
   return check_launch(c, "k_fft_x_tensor");
@@ -2134,7 +2137,7 @@ static int autotune_t(Ctx *c) {
     float ms = 0.f;
     for (int r = 0; r <= reps && st == IH_OK; ++r) {
       if (r == 1) cudaEventRecord(e0, c->stream);
-      st = tensor_last_pass(c, sp, c->y.fl, c->ytmp.fl, nullptr);
+      st = tensor_last_pass(c, sp, c->y.fl, c->ytmp.fl, c->ytmp.sc, nullptr);
     }
     if (st != IH_OK) break;
     cudaEventRecord(e1, c->stream);
@@ -2178,7 +2181,8 @@ int fft_autotune(Ctx *c) {
   template int fft_z_rhs_fused<T>(Ctx *, const C2<T> *, const T *, const double *, T *, T *,    \
                                   T *, C2<T> *, int, double *, int *, int);                     \
   template int fft_xy_roundtrip<T>(Ctx *, const C2<T> *, C2<T> *, C2<T> *, int);              \
-  template int fft_x_tensor<T>(Ctx *, const C2<T> *, const C2<T> *, T *, T *, const NextLin *);
+  template int fft_x_tensor<T>(Ctx *, const C2<T> *, const C2<T> *, T *, T *, double *,       \
+                               const NextLin *);
 IH_INST(float)
 IH_INST(double)
 #undef IH_INST

@@ -277,7 +277,7 @@ int fft_xy_roundtrip(Ctx *c, const C2<T> *z, C2<T> *d1, C2<T> *d2, int axis);
 // s45, stride M; z and y passes done) fused with update_h: writes the tensor
 // segments of out from those of y (toolbox.c:311-346, 363-397).
 template <typename T>
-int fft_x_tensor(Ctx *c, const C2<T> *s03, const C2<T> *s45, T *y, T *out,
+int fft_x_tensor(Ctx *c, const C2<T> *s03, const C2<T> *s45, T *y, T *out, double *outsc,
                  const NextLin *next);
 // Fused last inverse z pass for the RHS: c2r of the four derivative spectra,
 // then per point (grad phi)^2, rho, p (and their FP64 block sums), writes the
@@ -304,7 +304,8 @@ int fft_autotune(Ctx *c);
 // RHS and helpers (ih_rhs.cu)
 // the last forward x pass of the six S_ij spectra + update_h (either form);
 // next: also form the tensor segments of the next stage input (in y)
-int tensor_last_pass(Ctx *c, void *spec, void *y, void *out, const NextLin *next);
+int tensor_last_pass(Ctx *c, void *spec, void *y, void *out, double *outsc,
+                     const NextLin *next);
 int rhs(Ctx *c, double t, Vec &y, Vec &k, int filter, int output,
         const Vec *smry_src, const NextLin *next = nullptr);
 int reduce_mean(Ctx *c, const void *arr, long long n, double *dev_out);

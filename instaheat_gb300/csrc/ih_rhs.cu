@@ -311,10 +311,11 @@ __global__ void k_next_sc(const NextLin nl, const double *ksc, double *outsc) {
 template <typename T, bool NEXT>
 __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (NEXT ? 3 : 5) : 2)) k_update_h(
     const C2<T> *__restrict__ s, T *y, T *__restrict__ out, const RhsScalars *rs, Geom g,
-    const NextLin nl) {
+    const NextLin nl, double *outsc) {
   const long long M = g.M;
   const TensorConsts<T> tc(rs);
   const T dt = NEXT ? (T)*nl.dt : (T)0;
+  T mx = 0;
   const unsigned mz_magic = g.mz_magic;
   const int mz_shift = g.mz_shift, logny = g.logny;
   for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < M;
@@ -341,8 +342,9 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (NEXT ? 3 : 5) : 2)) k_
       ksq = q.ksq;
       tensor_sources<T>(m, q, v, n0, n1);
     }
-    tensor_eom<T, NEXT>(g, id, n0, n1, ksq, tc, y, out, nl, dt);
+    mx = fmax(mx, tensor_eom<T, NEXT>(g, id, n0, n1, ksq, tc, y, out, nl, dt));
   }
+  dh_max_store<T>(mx, outsc);
 }
 
 // The last forward x pass of the six S_ij spectra (arrays 0..3, 5, 6 of
@@ -351,28 +353,31 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (NEXT ? 3 : 5) : 2)) k_
 // autotuner chose (Ctx::tensor_fused).  next: the tensor entries of the next
 // stage input too (in y).
 template <typename T>
-static int tensor_last_pass_t(Ctx *c, C2<T> *s, T *y, T *out, const NextLin *next) {
+static int tensor_last_pass_t(Ctx *c, C2<T> *s, T *y, T *out, double *outsc,
+                              const NextLin *next) {
   const Geom &g = c->g;
   const long long M = g.M;
-  if (c->tensor_fused && g.pow2) return fft_x_tensor<T>(c, s, s + 5 * M, y, out, next);
+  if (c->tensor_fused && g.pow2) return fft_x_tensor<T>(c, s, s + 5 * M, y, out, outsc, next);
   IH_TRY((fft_xy<T>(c, s, M, 4, 0, -1)));
   IH_TRY((fft_xy<T>(c, s + 5 * M, M, 2, 0, -1)));
   const unsigned gm = grid_for(M, 256, 4);
   prof_begin(c, KK_UPDATE_H);
   if (next) {
-    k_update_h<T, true><<<gm, 256, 0, c->stream>>>(s, y, out, c->rs, g, *next);
+    k_update_h<T, true><<<gm, 256, 0, c->stream>>>(s, y, out, c->rs, g, *next, outsc);
   } else {
     NextLin none{};
-    k_update_h<T, false><<<gm, 256, 0, c->stream>>>(s, y, out, c->rs, g, none);
+    k_update_h<T, false><<<gm, 256, 0, c->stream>>>(s, y, out, c->rs, g, none, outsc);
   }
   prof_end(c, KK_UPDATE_H,
            6.0 * M * sizeof(C2<T>) + (8.0 + (next ? 4.0 * (next->n + 2) : 0.0)) * g.Next * sizeof(T));
   return check_launch(c, "k_update_h");
 }
-int tensor_last_pass(Ctx *c, void *spec, void *y, void *out, const NextLin *next) {
+int tensor_last_pass(Ctx *c, void *spec, void *y, void *out, double *outsc,
+                     const NextLin *next) {
   if (c->mixed)
-    return tensor_last_pass_t<float>(c, (C2<float> *)spec, (float *)y, (float *)out, next);
-  return tensor_last_pass_t<double>(c, (C2<double> *)spec, (double *)y, (double *)out, next);
+    return tensor_last_pass_t<float>(c, (C2<float> *)spec, (float *)y, (float *)out, outsc, next);
+  return tensor_last_pass_t<double>(c, (C2<double> *)spec, (double *)y, (double *)out, outsc,
+                                    next);
 }
 
 // ---------------------------------------------------------------------------
@@ -1005,7 +1010,7 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
     // (batched: per-array y-then-x ordering measured slower, no L2 reuse)
     IH_TRY((fft_xy<T>(c, spec, M, 4, 1, -1)));
     IH_TRY((fft_xy<T>(c, spec + 5 * M, M, 2, 1, -1)));
-    IH_TRY(tensor_last_pass(c, spec, yfl, kfl, next));
+    IH_TRY(tensor_last_pass(c, spec, yfl, kfl, k.sc, next));
   }
   // 6. phi/psi equations of motion (and the next stage input)
   prof_begin(c, KK_UPDATE_PHI_PSI);

@@ -199,9 +199,11 @@ __device__ __forceinline__ void nl_apply_c(const NextLin &nl, T dt, long long e,
 // zero mode) and k^2: h1' = dh1, h2' = dh2,
 // dh1' = -(2 <p> + k^2/a^2) h1 - 3 H dh1 + 2/a^2 n0 (and dh2'), reading the
 // tensor segments of y and writing those of out; NEXT: also the next stage's
-// input at the same entries of y (nl, dt = the step size in T).
+// input at the same entries of y (nl, dt = the step size in T).  Returns the
+// largest |component| of the two dh' values (the FP32 noise scale of the
+// tensor sources, see k_dopri_final).
 template <typename T, bool NEXT>
-__device__ __forceinline__ void tensor_eom(const Geom &g, long long id, C2<T> n0, C2<T> n1, T ksq,
+__device__ __forceinline__ T tensor_eom(const Geom &g, long long id, C2<T> n0, C2<T> n1, T ksq,
                                            const TensorConsts<T> &tc, T *y, T *__restrict__ out,
                                            const NextLin &nl, T dt) {
   const long long N = g.N, Next = g.Next;
@@ -228,6 +230,19 @@ __device__ __forceinline__ void tensor_eom(const Geom &g, long long id, C2<T> n0
     nl_apply_c<T>(nl, dt, e3, o3, yv);
     nl_apply_c<T>(nl, dt, e4, o4, yv);
   }
+  return fmax(fmax(fabs(o3.x), fabs(o3.y)), fmax(fabs(o4.x), fabs(o4.y)));
+}
+
+// the largest dh' of a k vector into its homogeneous slot 7 (zeroed by the
+// reduction-finish kernel of the same RHS): warp maximum, one atomic per warp
+template <typename T>
+__device__ __forceinline__ void dh_max_store(T mx, double *ksc) {
+  double v = (double)mx;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0 && v > 0.0)
+    atomicMax(reinterpret_cast<unsigned long long *>(ksc + 7),
+              (unsigned long long)__double_as_longlong(v));
 }
 
 }  // namespace ih
