@@ -1714,7 +1714,10 @@ int fft_zr2c(Ctx *c, const T *in, long long in_stride, C2<T> *out, long long out
              int count) {
   const Geom &g = c->g;
   prof_begin(c, KK_FFT_ZR2C);
-  if (g.h & (g.h - 1)) {
+  if (sizeof(T) == 4 && fused_wide_ok(c)) {
+    IH_TRY(zr2c_wide_launch(c, reinterpret_cast<const float *>(in), in_stride, out, out_stride,
+                            count));
+  } else if (g.h & (g.h - 1)) {
     const long long rows = (long long)g.nx * g.ny;
     const size_t sm = zg_smem<T>(g.h);
     cudaFuncSetAttribute(k_fft_zr2c_g<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);

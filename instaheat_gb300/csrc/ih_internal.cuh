@@ -291,6 +291,9 @@ int fft_z_rhs_fused(Ctx *c, const C2<T> *d4, const T *yfl, const double *ysc,
                     int *nblocks_out, int zsrc);
 // The same pass on the wide-row engine (ih_zwide.cu): mixed form, nz = 256.
 bool fused_wide_ok(const Ctx *c);
+// the plain r2c z pass on the wide-row engine (same condition)
+int zr2c_wide_launch(Ctx *c, const float *in, long long istride, void *out, long long ostride,
+                     int count);
 int fused_wide_launch(Ctx *c, const void *d4, const void *yfl, const double *ysc, void *lap,
                       void *p, void *rho, void *s6, int gw, double *partials, int *nblk_out,
                       int zsrc);

@@ -294,10 +294,64 @@ __global__ void __launch_bounds__(32 * kWarpsW, 4) k_fft_z_rhs_wide(
   }
 }
 
+// Plain r2c z pass on the wide-row engine (the z spectrum of phi in the
+// round-trip RHS, the filter's forward transforms): each lane loads its
+// reals 4t + 32q .. 4t + 32q + 3 of a row as float4s, one forward transform,
+// the r2c split, the row stored (t + 8m per lane, X_H by lane 0).
+struct WideR2cSmem {
+  float2 twh[kH];
+  float2 twz[2 * kH];
+  float2 xch[kWarpsW][kRowsW][kXch];
+};
+
+__global__ void __launch_bounds__(32 * kWarpsW) k_fft_zr2c_wide(const float *__restrict__ in,
+                                                               long long istride, float2 *out,
+                                                               long long ostride, long long rows,
+                                                               const float2 *__restrict__ twhg,
+                                                               const float2 *__restrict__ twzg) {
+  __shared__ WideR2cSmem sm;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int t = lane & 7, grp = lane >> 3, gbase = lane & ~7;
+  for (int i = tid; i < kH; i += blockDim.x) sm.twh[i] = twhg[i];
+  for (int i = tid; i < 2 * kH; i += blockDim.x) sm.twz[i] = twzg[i];
+  __syncthreads();
+  const long long row = ((long long)blockIdx.x * kWarpsW + warp) * kRowsW + grp;
+  const bool valid = row < rows;
+  const float *src = in + blockIdx.y * istride + row * (2 * kH) + 4 * t;
+  float2 v[16];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const float4 x = valid ? *reinterpret_cast<const float4 *>(src + 32 * q)
+                           : make_float4(0.f, 0.f, 0.f, 0.f);
+    v[2 * q] = make_float2(x.x, x.y);
+    v[2 * q + 1] = make_float2(x.z, x.w);
+  }
+  zw_forward(v, t, sm.xch[warp][grp], sm.twh);
+  float2 xH;
+  zw_r2c_post(v, t, gbase, sm.twz, xH);
+  if (valid) {
+    float2 *dst = out + blockIdx.y * ostride + row * (kH + 1);
+#pragma unroll
+    for (int m = 0; m < 16; ++m) dst[t + 8 * m] = v[m];
+    if (t == 0) dst[kH] = xH;
+  }
+}
+
 }  // namespace
 
 bool fused_wide_ok(const Ctx *c) {
   return c->mixed && c->zwide && c->g.h == kH;
+}
+
+int zr2c_wide_launch(Ctx *c, const float *in, long long istride, void *out, long long ostride,
+                     int count) {
+  const Geom &g = c->g;
+  const long long rows = (long long)g.nx * g.ny;
+  const long long per = (long long)kRowsW * kWarpsW;
+  k_fft_zr2c_wide<<<dim3((unsigned)((rows + per - 1) / per), count), 32 * kWarpsW, 0, c->stream>>>(
+      in, istride, reinterpret_cast<float2 *>(out), ostride, rows,
+      reinterpret_cast<const float2 *>(c->tw_h), reinterpret_cast<const float2 *>(c->tw_z));
+  return IH_OK;
 }
 
 int fused_wide_launch(Ctx *c, const void *d4, const void *yfl, const double *ysc, void *lap,
