@@ -49,8 +49,9 @@ enum { IH_PREC_F64 = 0, IH_PREC_MIXED = 1 };
 
 /* Grid and physics parameters: the parameters.sh keys of the hot path. */
 typedef struct {
-    int nx, ny, nz;        /* GRIDPOINTS_X/Y/Z: powers of two, nx >= ny >= nz >= 8,
-                              nx <= 256 (FP64) or 512 (mixed form) */
+    int nx, ny, nz;        /* GRIDPOINTS_X/Y/Z: 2^a 3^b (a >= 1; powers of two take
+                              the tuned engines, a factor 3 the mixed-radix route),
+                              nx >= ny >= nz >= 8, nx <= 256 (FP64) or 512 (mixed) */
     double lx, ly, lz;     /* SPATIAL_UPPER_BOUND_* - SPATIAL_LOWER_BOUND_* */
     double mass;           /* MASS (V = m^2 phi^2 / 2) */
     int enable_gw;         /* ENABLE_GW */
@@ -305,7 +306,7 @@ int ih_dopri853_set_proposer(ih_context *c, ih_mlp *m);
 /* ---- ensembles (no reference counterpart: the reference runs one
  * realization per process) ----
  * An ensemble owns `count` member contexts (each its own grid, box and
- * precision; powers of two as for ih_create) on one device.  Initial data
+ * precision; sizes as for ih_create) on one device.  Initial data
  * and outputs go through the member contexts (ih_ensemble_member).
  * ih_ensemble_run advances every member to tf with its own DOPRI853 step
  * sizes and controller (each member follows exactly the step sequence that
@@ -340,9 +341,11 @@ int ih_get_step_start_state(ih_context *c, double *f_host);
 /* Mixed form only: before an element of the two embedded error vectors enters
  * the FP64 error norm, its FP32 rounding floor eta * 2^-24 * sum_j |c_j k_j|
  * is subtracted from its magnitude (soft threshold), so that FP32 round-off
- * in the stage vectors does not drive the step size down.  Default eta = 256
- * in the mixed form; the plain FP64 form ignores it.  No reference
- * counterpart (the reference is FP64 only). */
+ * in the stage vectors does not drive the step size down; elements of the
+ * dh segment also drop eta * 2^-24 * sum_j |c_j| max|dh'_j| (the absolute
+ * noise the FP32 transforms of the tensor sources leave on every mode).
+ * Default eta = 256 in the mixed form; the plain FP64 form ignores it.  No
+ * reference counterpart (the reference is FP64 only). */
 int ih_dopri853_set_noise_floor(ih_context *c, double eta);
 /* Diagnostic: with diag on, every try also sums the squared scaled error
  * components per state segment; ih_dopri853_error_breakdown returns the last
