@@ -212,6 +212,17 @@ int ih_rhs_roundtrip(ih_context *c, int on);
  * update kernels that take on the combination stream up to 40 arrays at once
  * and run below the separate pass's bandwidth: at 256^3 it is slower. */
 int ih_stage_fusion(ih_context *c, int on);
+/* Velocity form of the DOPRI853 combinations in the mixed form (no
+ * reference counterpart; on by default, no effect in FP64).  The position
+ * half of every stage vector equals the velocity half of its stage input
+ * (phi' = dphi, psi' = dpsi, h' = dh; toolbox.c:282-299, 311-346), so the
+ * stage inputs, field_new and both error sums (dopri853.c:340-486) are formed
+ * from the velocity halves alone: Y^p = y^p + dt c y^v + dt^2 (A^2 k^v),
+ * field_new^p and the errors likewise with b^T A, e^T A (tableau products in
+ * FP64).  Equal to the reference's combinations in exact arithmetic; the
+ * position errors carry no rounding of the stage inputs.  Off: the
+ * reference's formulation, as the FP64 form always uses. */
+int ih_velocity_form(ih_context *c, int on);
 
 /* CUDA graphs (no reference counterpart): each DOPRI853 try (its 11 stage
  * combinations and RHS evaluations, the final combination and the error

@@ -522,6 +522,13 @@ int ih_stage_fusion(ih_context *h, int on) {
   return IH_OK;
 }
 
+int ih_velocity_form(ih_context *h, int on) {
+  CTX_CHECK(h);
+  h->c.velocity_form = on ? 1 : 0;
+  h->c.graph_epoch += 1;
+  return IH_OK;
+}
+
 int ih_rhs_roundtrip(ih_context *h, int on) {
   CTX_CHECK(h);
   h->c.roundtrip = on ? 1 : 0;
@@ -895,6 +902,7 @@ int ih_ensemble_autotune(ih_ensemble *e) {
       c->rt_var[1] = twin->rt_var[1];
       c->tensor_fused = twin->tensor_fused;
       c->zwide = twin->zwide;
+      c->velocity_form = twin->velocity_form;
       c->tune_report = twin->tune_report;
       c->graph_epoch += 1;
     } else {

@@ -213,6 +213,7 @@ struct Ctx {
   int tensor_fused = 0;  // update_h fused into the last x pass (autotuner's choice)
   int zwide = 1;         // the wide-row fused z pass where it applies (nz = 256, mixed)
   int stage_fusion = 0;  // DOPRI853 stage inputs formed by the RHS of the previous stage
+  int velocity_form = 1; // mixed form: stage combinations from the velocity halves only
   std::string tune_report;
 };
 

@@ -15,6 +15,7 @@
 #include <float.h>
 #include <math.h>
 #include <string.h>
+#include <mutex>
 #include "ih_internal.cuh"
 
 namespace ih {
@@ -439,6 +440,285 @@ static unsigned stream_grid(long long nvec) {
   return (unsigned)b;
 }
 
+// ---------------------------------------------------------------------------
+// Velocity form of the stage combinations (the mixed form).  Three pairs of
+// state segments are (position, velocity) with position' = velocity in the
+// RHS -- (phi, Pi), (psi, dpsi), (h, dh), toolbox.c:282-299, 311-346 -- so
+// the position half of every stage vector is the velocity half of its stage
+// input, k_j^p = Y_j^v = y^v + dt sum_l a_jl k_l^v.  Hence
+//   Y_s^p  = y^p + dt (sum_j a_sj) y^v + dt^2 sum_l (A^2)_sl k_l^v,
+//   ynew^p = y^p + dt (sum_j b_j) y^v + dt^2 sum_l (b^T A)_l k_l^v,
+//   err^p  = (sum_j e_j) y^v + dt sum_l (e^T A)_l k_l^v   (e = e5, e3),
+// the reference's combinations (dopri853.c:340-486) in exact arithmetic, with
+// only the velocity halves of the stage vectors read (about 13 GB less per
+// try at 256^3).  The FP64 form keeps the reference's formulation.
+
+// position / velocity element pairs, W at a time (region boundaries are
+// multiples of W): (phi, Pi), (psi, dpsi) over N, (h1, dh1), (h2, dh2) over
+// Next; segment classes 0 phi, 1 Pi, 2 psi, 3 dpsi, 4 h, 5 dh
+__device__ __forceinline__ void vel_pair(long long q, long long N, long long Next, long long &ip,
+                                         long long &iv, int &cp, int &cv) {
+  if (q < N) {
+    ip = q;
+    iv = N + q;
+    cp = 0;
+    cv = 1;
+  } else if (q < 2 * N) {
+    ip = N + q;
+    iv = 2 * N + q;
+    cp = 2;
+    cv = 3;
+  } else if (q < 2 * N + Next) {
+    const long long e = q - 2 * N;
+    ip = 4 * N + e;
+    iv = 4 * N + 2 * Next + e;
+    cp = 4;
+    cv = 5;
+  } else {
+    const long long e = q - 2 * N - Next;
+    ip = 4 * N + Next + e;
+    iv = 4 * N + 3 * Next + e;
+    cp = 4;
+    cv = 5;
+  }
+}
+
+struct VelLin {
+  const void *k[kMaxTerms];       // stage vectors (velocity halves read)
+  const double *ksc[kMaxTerms];
+  double cv[kMaxTerms];           // a_sl (velocity; the homogeneous parts)
+  float cvf[kMaxTerms], cpf[kMaxTerms];  // a_sl and (A^2)_sl in FP32
+  float csf;                      // sum_l a_sl
+  int n;
+  const double *dt;
+};
+
+__global__ void k_lincomb_vel(const float *__restrict__ y, const double *ysc,
+                              float *__restrict__ out, double *outsc, const VelLin a, long long N,
+                              long long Next) {
+  const long long nq = (2 * N + 2 * Next) / 4;
+  const double dtd = *a.dt;
+  const float dt = (float)dtd;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nq;
+       v += (long long)gridDim.x * blockDim.x) {
+    long long ip, iv;
+    int c0, c1;
+    vel_pair(v * 4, N, Next, ip, iv, c0, c1);
+    float av[4] = {0.f, 0.f, 0.f, 0.f}, ap[4] = {0.f, 0.f, 0.f, 0.f}, x[4];
+#pragma unroll
+    for (int j = 0; j < kMaxTerms; ++j) {
+      if (j < a.n) {
+        vload<float>((const float *)a.k[j] + iv, x);
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+          av[w] += a.cvf[j] * x[w];
+          ap[w] += a.cpf[j] * x[w];
+        }
+      }
+    }
+    float yp[4], yv[4], op[4], ov[4];
+    vload<float>(y + ip, yp);
+    vload<float>(y + iv, yv);
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      ov[w] = yv[w] + dt * av[w];
+      op[w] = yp[w] + dt * (a.csf * yv[w] + dt * ap[w]);
+    }
+    vstore<float>(out + iv, ov);
+    vstore<float>(out + ip, op);
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 5) {
+    const int s = threadIdx.x;
+    double acc = 0.0;
+    for (int j = 0; j < a.n; ++j) acc += a.cv[j] * a.ksc[j][s];
+    outsc[s] = ysc[s] + dtd * acc;
+  }
+}
+
+constexpr int kFinalVelStages = 10;  // DOPRI853 stages 1, 4..12
+
+struct FinalVel {
+  const void *k[12];              // the stages with a nonzero coefficient
+  const double *ksc[12];
+  double b[12], e5[12], e3[12];   // velocity weights (and the homogeneous parts)
+  float bf[12], e5f[12], e3f[12];
+  float bpf[12], e5pf[12], e3pf[12];  // (b^T A)_l, (e5^T A)_l, (e3^T A)_l
+  float sbf, s5f, s3f;            // sum_l b_l, e5_l, e3_l
+  int n;
+  const double *dt;
+  double rtol, atol, noise;
+  long long next;
+  double *diag;
+};
+
+// NS = a.n stages (10 for DOPRI853: stages 1, 4..12), all loads of an
+// element group issued before its arithmetic
+template <int NS, bool DIAG>
+__global__ void __launch_bounds__(256, 2) k_dopri_final_vel(const float *__restrict__ y, const double *ysc,
+                                  float *__restrict__ ynew, double *ynsc, const FinalVel a,
+                                  long long N, double *partials) {
+  __shared__ double hs[5][5];
+  const double dt = *a.dt;
+  if (threadIdx.x < 5) {  // homogeneous parts: full weights on every stage's scalars
+    const int sidx = threadIdx.x;
+    double x = 0.0, e5 = 0.0, e3 = 0.0;
+    for (int j = 0; j < a.n; ++j) {
+      const double kv = a.ksc[j][sidx];
+      x += a.b[j] * kv;
+      e5 += a.e5[j] * kv;
+      e3 += a.e3[j] * kv;
+    }
+    hs[0][sidx] = x;
+    hs[1][sidx] = e5;
+    hs[2][sidx] = e3;
+    hs[3][sidx] = ysc[sidx];
+    hs[4][sidx] = ysc[sidx] + dt * x;
+  }
+  __syncthreads();
+  const float dtf = (float)dt;
+  const float atolf = (float)a.atol, rtolf = (float)a.rtol, nz = (float)a.noise;
+  // absolute floors from max|dh'| of each stage (slot 7): dh (velocity) and h
+  float nab5v = 0.f, nab3v = 0.f, nab5p = 0.f, nab3p = 0.f;
+  for (int j = 0; j < a.n; ++j) {
+    const float mj = (float)a.ksc[j][7];
+    nab5v += fabsf(a.e5f[j]) * mj;
+    nab3v += fabsf(a.e3f[j]) * mj;
+    nab5p += fabsf(a.e5pf[j]) * mj;
+    nab3p += fabsf(a.e3pf[j]) * mj;
+  }
+  nab5v *= nz;
+  nab3v *= nz;
+  nab5p *= nz * dtf;
+  nab3p *= nz * dtf;
+  const long long Next = a.next;
+  const long long nq = (2 * N + 2 * Next) / 4;
+  double err = 0.0, err2 = 0.0;
+  double dacc[DIAG ? 12 : 1];
+#pragma unroll
+  for (int i = 0; i < (DIAG ? 12 : 1); ++i) dacc[i] = 0.0;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nq;
+       v += (long long)gridDim.x * blockDim.x) {
+    long long ip, iv;
+    int c0, c1;
+    vel_pair(v * 4, N, Next, ip, iv, c0, c1);
+    float4 xs[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) xs[j] = *reinterpret_cast<const float4 *>((const float *)a.k[j] + iv);
+    float yp[4], yv[4], np[4], nv[4];
+    vload<float>(y + ip, yp);
+    vload<float>(y + iv, yv);
+    float bv[4] = {}, f5v[4] = {}, f3v[4] = {}, t5v[4] = {}, t3v[4] = {};
+    float bp[4] = {}, f5p[4] = {}, f3p[4] = {}, t5p[4] = {}, t3p[4] = {};
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      const float x[4] = {xs[j].x, xs[j].y, xs[j].z, xs[j].w};
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        bv[w] += a.bf[j] * x[w];
+        f5v[w] += a.e5f[j] * x[w];
+        f3v[w] += a.e3f[j] * x[w];
+        t5v[w] += fabsf(a.e5f[j] * x[w]);
+        t3v[w] += fabsf(a.e3f[j] * x[w]);
+        bp[w] += a.bpf[j] * x[w];
+        f5p[w] += a.e5pf[j] * x[w];
+        f3p[w] += a.e3pf[j] * x[w];
+        t5p[w] += fabsf(a.e5pf[j] * x[w]);
+        t3p[w] += fabsf(a.e3pf[j] * x[w]);
+      }
+    }
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      nv[w] = yv[w] + dtf * bv[w];
+      np[w] = yp[w] + dtf * (a.sbf * yv[w] + dtf * bp[w]);
+      // position errors: the y^v terms, then dt times the stage sums
+      const float g5 = a.s5f * yv[w], g3 = a.s3f * yv[w];
+      f5p[w] = g5 + dtf * f5p[w];
+      f3p[w] = g3 + dtf * f3p[w];
+      t5p[w] = fabsf(g5) + dtf * t5p[w];
+      t3p[w] = fabsf(g3) + dtf * t3p[w];
+    }
+    vstore<float>(ynew + iv, nv);
+    vstore<float>(ynew + ip, np);
+    // the two elements of each pair: FP32 rounding floors removed, FP64 norm
+    double acc5[2] = {0.0, 0.0}, acc3[2] = {0.0, 0.0};
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int cls = half ? c1 : c0;
+      const int seg = cls < 4 ? cls : 4;
+      const float ys = seg < 4 ? (float)hs[3][seg] : 0.f, yns = seg < 4 ? (float)hs[4][seg] : 0.f;
+      const float q5s = seg < 4 ? (float)hs[1][seg] : 0.f, q3s = seg < 4 ? (float)hs[2][seg] : 0.f;
+      const float fa5 = cls == 5 ? nab5v : (cls == 4 ? nab5p : 0.f);
+      const float fa3 = cls == 5 ? nab3v : (cls == 4 ? nab3p : 0.f);
+      float a5s = 0.f, a3s = 0.f;
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const float e5 = half ? f5v[w] : f5p[w], e3 = half ? f3v[w] : f3p[w];
+        const float s5 = half ? t5v[w] : t5p[w], s3 = half ? t3v[w] : t3p[w];
+        const float yo = half ? yv[w] : yp[w], yn = half ? nv[w] : np[w];
+        const float r5a = fmaxf(fabsf(e5) - nz * s5 - fa5, 0.f);
+        const float r3a = fmaxf(fabsf(e3) - nz * s3 - fa3, 0.f);
+        const float q5 = copysignf(r5a, e5) + q5s, q3 = copysignf(r3a, e3) + q3s;
+        const float isk = __frcp_rn(atolf + rtolf * fmaxf(fabsf(ys + yo), fabsf(yns + yn)));
+        const float r5 = q5 * isk, r3 = q3 * isk;
+        a5s += r5 * r5;
+        a3s += r3 * r3;
+      }
+      acc5[half] = (double)a5s;
+      acc3[half] = (double)a3s;
+    }
+    err2 += acc5[0] + acc5[1];
+    err += acc3[0] + acc3[1];
+    if constexpr (DIAG) {
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        if (q == c0) {
+          dacc[2 * q] += acc5[0];
+          dacc[2 * q + 1] += acc3[0];
+        }
+        if (q == c1) {
+          dacc[2 * q] += acc5[1];
+          dacc[2 * q + 1] += acc3[1];
+        }
+      }
+    }
+  }
+  if constexpr (DIAG) {
+#pragma unroll
+    for (int i = 0; i < 12; ++i)
+      if (dacc[i] != 0.0) atomicAdd(&a.diag[i], dacc[i]);
+  }
+  // scale factor a (the last state component), the new homogeneous parts
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const double sk = a.atol + a.rtol * fmax(fabs(hs[3][4]), fabs(hs[4][4]));
+    const double r5 = hs[1][4] / sk, r3 = hs[2][4] / sk;
+    err2 += r5 * r5;
+    err += r3 * r3;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) ynsc[q] = hs[4][q];
+    ynsc[5] = ynsc[6] = ynsc[7] = 0.0;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    err += __shfl_down_sync(0xffffffffu, err, o);
+    err2 += __shfl_down_sync(0xffffffffu, err2, o);
+  }
+  __shared__ double red[2][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][wid] = err;
+    red[1][wid] = err2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double e = 0.0, e2 = 0.0;
+    for (int w = 0; w < (int)(blockDim.x / 32); ++w) {
+      e += red[0][w];
+      e2 += red[1][w];
+    }
+    partials[2 * blockIdx.x] = e;
+    partials[2 * blockIdx.x + 1] = e2;
+  }
+}
+
 static int lincomb(Ctx *c, const Vec &base, Vec &out, const LinArgs &args) {
   const long long nf = c->g.Nf;
   prof_begin(c, KK_LINCOMB);
@@ -533,6 +813,135 @@ int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0, int want_
 // combinations and RHS evaluations, the final combination and the two error
 // sums, reduced into diag[48..50] (error(), <rho>, the NaN flag).  The step
 // size is read from c->dt_dev, so one capture serves every try.
+// Tableau products of the velocity form (FP64, once): row s of try_body
+// (stage s+1 from stages 1..s): VCS[s] = sum_j a_sj, VAA[s][l] =
+// sum_{j=l+1}^{s-1} a_sj a_jl; final weights per stage i (0-based) and their
+// products with the tableau, VBA[l] = sum_{j>l} b_j a_jl (and e5, e3).
+static double VAA[12][12], VCS[12], VB[12], VE5[12], VE3[12], VBA[12], VE5A[12], VE3A[12];
+static double VSB, VS5, VS3;
+static std::once_flag vel_once;
+static void vel_tables() {
+  std::call_once(vel_once, [] {
+    tableau_init();
+    memset(VAA, 0, sizeof VAA);
+    for (int s = 1; s < 12; ++s) {
+      double cs = 0.0;
+      for (int j = 0; j < s; ++j) cs += DA[s][j];
+      VCS[s] = cs;
+      for (int l = 0; l + 1 < s; ++l) {
+        double q = 0.0;
+        for (int j = l + 1; j < s; ++j) q += DA[s][j] * DA[j][l];
+        VAA[s][l] = q;
+      }
+    }
+    VSB = VS5 = VS3 = 0.0;
+    for (int i = 0; i < 12; ++i) {
+      const double bhh = i == 0 ? DBHH[0] : (i == 8 ? DBHH[1] : (i == 11 ? DBHH[2] : 0.0));
+      VB[i] = DB[i];
+      VE5[i] = DB[i] - bhh;
+      VE3[i] = DE3[i];
+      VSB += VB[i];
+      VS5 += VE5[i];
+      VS3 += VE3[i];
+    }
+    for (int l = 0; l < 12; ++l) {
+      double b = 0.0, e5 = 0.0, e3 = 0.0;
+      for (int j = l + 1; j < 12; ++j) {
+        b += VB[j] * DA[j][l];
+        e5 += VE5[j] * DA[j][l];
+        e3 += VE3[j] * DA[j][l];
+      }
+      VBA[l] = b;
+      VE5A[l] = e5;
+      VE3A[l] = e3;
+    }
+  });
+}
+
+// the input of stage s+1 in the velocity form (mixed form)
+static int lincomb_vel(Ctx *c, int s) {
+  vel_tables();
+  VelLin a;
+  memset(&a, 0, sizeof a);
+  int n = 0;
+  for (int l = 0; l < s; ++l) {
+    if (DA[s][l] == 0.0 && VAA[s][l] == 0.0) continue;
+    a.k[n] = c->k[l + 1].fl;
+    a.ksc[n] = c->k[l + 1].sc;
+    a.cv[n] = DA[s][l];
+    a.cvf[n] = (float)DA[s][l];
+    a.cpf[n] = (float)VAA[s][l];
+    ++n;
+  }
+  a.n = n;
+  a.csf = (float)VCS[s];
+  a.dt = c->dt_dev;
+  const Geom &g = c->g;
+  const long long nq = (2 * g.N + 2 * g.Next) / 4;
+  prof_begin(c, KK_LINCOMB);
+  k_lincomb_vel<<<stream_grid(nq), 256, 0, c->stream>>>((const float *)c->y.fl, c->y.sc,
+                                                        (float *)c->ytmp.fl, c->ytmp.sc, a, g.N,
+                                                        g.Next);
+  prof_end(c, KK_LINCOMB, (double)(n + 4) * (g.Nf / 2) * sizeof(float));
+  return check_launch(c, "k_lincomb_vel");
+}
+
+// field_new and both error sums in the velocity form (mixed form)
+static int final_vel(Ctx *c) {
+  vel_tables();
+  FinalVel f;
+  memset(&f, 0, sizeof f);
+  int n = 0;
+  for (int i = 0; i < 12; ++i) {
+    if (VB[i] == 0.0 && VE5[i] == 0.0 && VE3[i] == 0.0 && VBA[i] == 0.0 && VE5A[i] == 0.0 &&
+        VE3A[i] == 0.0)
+      continue;
+    f.k[n] = c->k[i + 1].fl;
+    f.ksc[n] = c->k[i + 1].sc;
+    f.b[n] = VB[i];
+    f.e5[n] = VE5[i];
+    f.e3[n] = VE3[i];
+    f.bf[n] = (float)VB[i];
+    f.e5f[n] = (float)VE5[i];
+    f.e3f[n] = (float)VE3[i];
+    f.bpf[n] = (float)VBA[i];
+    f.e5pf[n] = (float)VE5A[i];
+    f.e3pf[n] = (float)VE3A[i];
+    ++n;
+  }
+  if (n != kFinalVelStages) {  // fixed by the tableau
+    c->err = "velocity form: unexpected stage count of the final combination";
+    return IH_ERR_STATE;
+  }
+  f.n = n;
+  f.sbf = (float)VSB;
+  f.s5f = (float)VS5;
+  f.s3f = (float)VS3;
+  f.dt = c->dt_dev;
+  f.rtol = c->cfg.rtol;
+  f.atol = c->cfg.atol;
+  f.noise = c->noise_eta * 5.9604644775390625e-8;  // eta * 2^-24
+  f.next = c->g.Next;
+  f.diag = nullptr;
+  if (c->err_diag) {
+    f.diag = c->diag + 4 * c->g.bins + 64 + 8;  // 12 doubles
+    IH_CUDA(c, cudaMemsetAsync(f.diag, 0, sizeof(double) * 12, c->stream));
+  }
+  const Geom &g = c->g;
+  const long long nq = (2 * g.N + 2 * g.Next) / 4;
+  const unsigned nb = stream_grid(nq);
+  prof_begin(c, KK_DOPRI_FINAL);
+  auto kf = f.diag ? k_dopri_final_vel<kFinalVelStages, true>
+                    : k_dopri_final_vel<kFinalVelStages, false>;
+  kf<<<nb, 256, 0, c->stream>>>((const float *)c->y.fl, c->y.sc, (float *)c->ynew.fl, c->ynew.sc,
+                                f, g.N, c->partials);
+  prof_end(c, KK_DOPRI_FINAL, (double)(n + 4) * (g.Nf / 2) * sizeof(float));
+  IH_TRY(check_launch(c, "k_dopri_final_vel"));
+  k_dopri_err_finish<<<1, 256, 0, c->stream>>>(c->partials, (int)nb, c->dt_dev, (double)g.Ntot,
+                                               c->rs, c->diag + 4 * g.bins + 48);
+  return check_launch(c, "k_dopri_err_finish");
+}
+
 // The combination forming the input of iteration s of try_body (stage s+1)
 // from stages 1..s, without the term of stage s when `self` is given: that
 // term then comes from the RHS that writes stage s (NextLin).
@@ -573,9 +982,13 @@ static int try_body(Ctx *c) {
   // of the stage vector and one launch fewer per stage.
   // (not with the fused tensor x pass, whose variants with and without the
   // combination do not round identically)
-  const bool fuse = c->stage_fusion && !c->tensor_fused;
+  // (the mixed form combines stages in the velocity form instead)
+  const bool vel = c->mixed && c->velocity_form;
+  const bool fuse = c->stage_fusion && !c->tensor_fused && !vel;
   for (int s = 1; s < 12; ++s) {  // stage s+1 from stages 1..s
-    if (s == 1 || !fuse) {  // else the previous stage's RHS formed it
+    if (vel) {
+      IH_TRY(lincomb_vel(c, s));
+    } else if (s == 1 || !fuse) {  // else the previous stage's RHS formed it
       LinArgs a;
       memset(&a, 0, sizeof a);
       stage_terms(c, s, false, &a, nullptr);
@@ -588,6 +1001,7 @@ static int try_body(Ctx *c) {
     // the RHS does not depend on t explicitly (toolbox.c:75-88)
     IH_TRY(rhs(c, 0.0, c->ytmp, c->k[s + 1], 0, 0, nullptr, fuse_next ? &nl : nullptr));
   }
+  if (vel) return final_vel(c);
   FinalArgs f;
   memset(&f, 0, sizeof f);
   const int st[8] = {1, 6, 7, 8, 9, 10, 11, 12};

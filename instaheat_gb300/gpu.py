@@ -156,6 +156,7 @@ def load(build_if_missing: bool = True):
     L.ih_graphs_enable.argtypes = [vp, C.c_int]
     L.ih_rhs_roundtrip.argtypes = [vp, C.c_int]
     L.ih_stage_fusion.argtypes = [vp, C.c_int]
+    L.ih_velocity_form.argtypes = [vp, C.c_int]
     L.ih_ensemble_create.argtypes = [C.POINTER(Params), C.c_int, C.POINTER(vp)]
     L.ih_ensemble_destroy.argtypes = [vp]
     L.ih_ensemble_destroy.restype = None
@@ -384,6 +385,12 @@ class Context:
         (on) or by separate combination passes (off, the default); the results
         are identical to the bit."""
         self._ck(self.L_.ih_stage_fusion(self.h, int(on)), "ih_stage_fusion")
+
+    def velocity_form(self, on=True):
+        """Mixed form: DOPRI853 combinations from the velocity halves of the
+        stage vectors (on, the default) or the reference's formulation (off).
+        No effect in FP64."""
+        self._ck(self.L_.ih_velocity_form(self.h, int(on)), "ih_velocity_form")
 
     def engines(self):
         """Engines of the x, y, fused x passes, the x, y round trips, the form

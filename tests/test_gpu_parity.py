@@ -177,11 +177,14 @@ def test_mixed_rhs_against_f64_oracle(gpu_mod, oracle_mod):
     assert abs(r_gpu[-1] - r_ref[-1]) <= 1e-10 * abs(r_ref[-1])
 
 
-def test_mixed_dopri_tracks_f64(gpu_mod, oracle_mod):
-    """Five mixed-form DOPRI853 steps stay within 1e-7 (relative to each
-    segment's fluctuation scale) of the FP64 oracle at rtol 1e-8."""
+@pytest.mark.parametrize("velocity_form", [True, False])
+def test_mixed_dopri_tracks_f64(gpu_mod, oracle_mod, velocity_form):
+    """Five mixed-form DOPRI853 steps stay within 1e-4 (relative to each
+    segment's fluctuation scale) of the FP64 oracle at rtol 1e-8, with the
+    combinations in the velocity form (the default) or the reference's."""
     n = (32, 32, 32)
     ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
+    ctx.velocity_form(velocity_form)
     o = oracle_mod.Oracle(n=n)
     f = o.ic(seed=8, amp=1e-3)
     cfg_o = oracle_mod.default_cfg(1e-8, 1e-8, 1e-2)
@@ -393,6 +396,7 @@ def test_stage_fusion_bit_identical(gpu_mod, prec, tensor_fused):
     for fuse in (False, True):
         ctx = gpu_mod.Context(n=n, precision=precision)
         ctx.set_engine(5, tensor_fused)
+        ctx.velocity_form(False)  # the mixed form fuses only in the reference's form
         ctx.stage_fusion(fuse)
         ctx.ic(seed=31, amp=1e-3)
         ctx.dopri_init(gpu_mod.dopri_cfg(1e-8, 1e-8), 0.0, 1e-2)
