@@ -203,7 +203,8 @@ def bench_form(gpu, precision, device, seed, steps, warmup, profile=False, clock
            "fft_engines": dict(zip(("x", "y", "deriv4_x", "roundtrip_x", "roundtrip_y"),
                                    (ENGINE_NAMES[e] for e in ctx.engines()[:5])))
                           | {"tensor_x": ("fused" if ctx.engines()[5] else "separate"),
-                             "z_fused": ("wide rows" if ctx.engines()[6] else "warp rows")},
+                             "z_fused": ("wide rows" if ctx.engines()[6] else "warp rows"),
+                             "gw_yx_slab": ctx.engines()[7]},
            "fft_autotune": ctx.autotune_report}
     return ctx, res
 

@@ -174,9 +174,9 @@ int ih_variance_host(ih_context *c, double mean, const double *f_host, size_t n,
 /* ---- FFT autotuner (no reference counterpart; FFTW's planner flag
  * FFTW_DEFAULT_FLAG, parameters.sh, plays this role there) ----
  * Times every engine variant of the x and y passes, of the fused inverse x
- * pass, of the x and y derivative round trips and of the last tensor x pass
- * of the RHS on the context's scratch spectra and keeps the fastest per
- * pass.  Until it is called the passes use the shared-memory Stockham
+ * pass, of the x and y derivative round trips, of the last tensor x pass and
+ * the kz slab widths of the tensor sources' y/x passes of the RHS on the
+ * context's scratch spectra and keeps the fastest per pass.  Until it is called the passes use the shared-memory Stockham
  * engine.  Results are identical across variants up to rounding.  The report
  * lists the timings and the choice (valid until the next ih_autotune). */
 int ih_autotune(ih_context *c);
@@ -186,7 +186,11 @@ const char *ih_autotune_report(const ih_context *c);
  * only), 5 = the last x pass of the tensor sources (0 = x passes then
  * update_h, 1 = one kernel accumulating the TT projection), 6 = the fused z
  * pass of the RHS (1 = the wide-row engine, 8 lanes x 16 values per row, where
- * it applies: mixed form, nz = 256 -- the default; 0 = a warp per row);
+ * it applies: mixed form, nz = 256 -- the default; 0 = a warp per row), 7 =
+ * the kz slab width of the forward y and x passes of the six tensor sources
+ * (0 = whole arrays, the default; a multiple of 8 up to 64 = y then x pass on
+ * one slab of all six at a time, so the slab stays in L2 between the two; it
+ * applies with pass 5 = 0);
  * engine IH_FFT_STOCKHAM, IH_FFT_TWOSTEP (register two-step,
  * 128-byte tiles), IH_FFT_TWOSTEP_HALF (64-byte tiles), IH_FFT_PIPELINED
  * (register two-step in persistent CTAs that copy the next tile in with

@@ -495,6 +495,12 @@ const char *ih_autotune_report(const ih_context *h) {
 
 int ih_fft_set_engine(ih_context *h, int pass, int engine) {
   CTX_CHECK(h);
+  if (pass == 7) {  // kz slab width of the tensor sources' y/x passes
+    if (engine < 0 || engine > 64 || engine % 8) return IH_ERR_ARG;
+    h->c.gw_slab = engine;
+    h->c.graph_epoch += 1;
+    return IH_OK;
+  }
   if (pass < 0 || pass > 6 || engine < 0 || engine >= FV_COUNT) return IH_ERR_ARG;
   if (pass == 2 && engine == FV_THREESTEP) return IH_ERR_ARG;
   if ((pass == 3 || pass == 4) && engine != FV_TWOSTEP && engine != FV_TWOSTEP_HALF)
@@ -543,7 +549,8 @@ int ih_graphs_enable(ih_context *h, int on) {
 }
 
 int ih_fft_get_engine(const ih_context *h, int pass) {
-  if (!h || pass < 0 || pass > 6) return -1;
+  if (!h || pass < 0 || pass > 7) return -1;
+  if (pass == 7) return h->c.gw_slab;
   if (pass < 2) return h->c.xy_var[pass];
   if (pass == 5) return h->c.tensor_fused;
   if (pass == 6) return h->c.zwide;
@@ -902,6 +909,7 @@ int ih_ensemble_autotune(ih_ensemble *e) {
       c->rt_var[1] = twin->rt_var[1];
       c->tensor_fused = twin->tensor_fused;
       c->zwide = twin->zwide;
+      c->gw_slab = twin->gw_slab;
       c->velocity_form = twin->velocity_form;
       c->tune_report = twin->tune_report;
       c->graph_epoch += 1;

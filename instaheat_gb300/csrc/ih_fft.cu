@@ -1581,13 +1581,15 @@ struct XYLaunch {
   C2<T> *data;
   long long stride;
   int count, axis, sign, var;
+  int cols = 0;  // columns (kz values) from data on: 0 = all mz of the plane
+  int mzv() const { return cols ? cols : c->g.mz; }
   template <int B, bool GEN = false>
   int run_st(int L, dim3 grid, long long sj, long long so, const C2<T> *tw) {
     const size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * (B + 1));
     cudaFuncSetAttribute(k_fft_xy_st<T, B, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sm);
     k_fft_xy_st<T, B, GEN><<<grid, threads_st(L, B), sm, c->stream>>>(data, stride, L, sj, so,
-                                                                       c->g.mz, sign, tw);
+                                                                       mzv(), sign, tw);
     return IH_OK;
   }
   template <int L, int B>
@@ -1595,7 +1597,7 @@ struct XYLaunch {
     const size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * B);
     cudaFuncSetAttribute(k_fft_xy_2s<T, L, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_fft_xy_2s<T, L, B><<<grid, pass_threads<L, B>(), sm, c->stream>>>(data, stride, sj, so,
-                                                                         c->g.mz, sign, tw);
+                                                                         mzv(), sign, tw);
     return IH_OK;
   }
   template <int L, int B>
@@ -1612,7 +1614,7 @@ struct XYLaunch {
           occ < 1)
         occ = 1;
     }
-    XYTiles tl{stride, so, g.mz, (g.mz + B - 1) / B, outer};
+    XYTiles tl{stride, so, mzv(), (mzv() + B - 1) / B, outer};
     const long long total = (long long)tl.ntz * outer * count;
     const long long cap = (long long)occ * c->num_sms;
     const unsigned nb = (unsigned)(total < cap ? total : cap);
@@ -1623,7 +1625,7 @@ struct XYLaunch {
   int run_3s(dim3 grid, long long sj, long long so, const C2<T> *tw) {
     const size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * B);
     cudaFuncSetAttribute(k_fft_xy_3s<T, L, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_fft_xy_3s<T, L, B><<<grid, threads3<L, B>(), sm, c->stream>>>(data, stride, sj, so, c->g.mz,
+    k_fft_xy_3s<T, L, B><<<grid, threads3<L, B>(), sm, c->stream>>>(data, stride, sj, so, mzv(),
                                                                      sign, tw);
     return IH_OK;
   }
@@ -1639,15 +1641,16 @@ struct XYLaunch {
       const int outer = axis == 0 ? g.ny : g.nx;
       const C2<T> *tw = tab<T>(axis == 0 ? c->tw_x : c->tw_y);
       if (var == FV_PIPELINED) return run_pipe<L, B>(sj, so, outer, tw);
+      const int mz = mzv();
       if (var == FV_THREESTEP) {
         if constexpr (L >= 64) {
-          return run_3s<L, B>(dim3((g.mz + B - 1) / B, outer, count), sj, so, tw);
+          return run_3s<L, B>(dim3((mz + B - 1) / B, outer, count), sj, so, tw);
         } else {  // short pencils: the two-step engine already holds <= 8 values
-          return run_2s<L, B>(dim3((g.mz + B - 1) / B, outer, count), sj, so, tw);
+          return run_2s<L, B>(dim3((mz + B - 1) / B, outer, count), sj, so, tw);
         }
       }
       const int bw = var == FV_TWOSTEP_HALF ? B / 2 : B;
-      dim3 grid((g.mz + bw - 1) / bw, outer, count);
+      dim3 grid((mz + bw - 1) / bw, outer, count);
       if (var == FV_TWOSTEP) return run_2s<L, B>(grid, sj, so, tw);
       if (var == FV_TWOSTEP_HALF) return run_2s<L, B / 2>(grid, sj, so, tw);
       return run_st<B>(L, grid, sj, so, tw);
@@ -1674,6 +1677,42 @@ int fft_xy(Ctx *c, C2<T> *data, long long stride, int count, int axis, int sign)
   }
   prof_end(c, KK_FFT_XY, 2.0 * count * g.M * sizeof(C2<T>));
   return check_launch(c, "k_fft_xy");
+}
+
+// The forward y then x passes of the six S_ij spectra (arrays 0..3 and 5, 6
+// of spec), kz slab by kz slab when w > 0: a slab of the six arrays (6 nx ny w
+// complex values, 50 MB at 256^2 x 16 in FP32) stays in L2 between its y and
+// its x pass, so the x pass reads it from L2 and the y pass's writes are
+// overwritten there before they reach HBM.  w = 0: whole arrays (y passes,
+// then x passes).  The last slab takes the remainder (w to 2w - 1 columns).
+template <typename T>
+int fft_gw_yx(Ctx *c, C2<T> *spec, int w) {
+  const Geom &g = c->g;
+  const long long M = g.M;
+  if (w <= 0 || !g.pow2 || w >= g.mz) {
+    IH_TRY((fft_xy<T>(c, spec, M, 4, 1, -1)));
+    IH_TRY((fft_xy<T>(c, spec + 5 * M, M, 2, 1, -1)));
+    IH_TRY((fft_xy<T>(c, spec, M, 4, 0, -1)));
+    return fft_xy<T>(c, spec + 5 * M, M, 2, 0, -1);
+  }
+  const int ns = g.mz / w;
+  for (int q = 0; q < ns; ++q) {
+    const int z0 = q * w, ws = (q + 1 < ns) ? w : g.mz - z0;
+    for (int axis = 1; axis >= 0; --axis) {
+      for (int grp = 0; grp < 2; ++grp) {
+        const int count = grp ? 2 : 4;
+        C2<T> *d = spec + (grp ? 5 * M : 0) + z0;
+        const int L = axis == 0 ? g.nx : g.ny;
+        prof_begin(c, KK_FFT_XY);
+        XYLaunch<T> xl{c, d, M, count, axis, -1, c->xy_var[axis]};
+        xl.cols = ws;
+        IH_TRY(dispatch_len(L, xl, allow512<T>()));
+        prof_end(c, KK_FFT_XY, 2.0 * count * (double)g.nx * g.ny * ws * sizeof(C2<T>));
+        IH_TRY(check_launch(c, "k_fft_xy"));
+      }
+    }
+  }
+  return IH_OK;
 }
 
 template <typename T>
@@ -1907,7 +1946,8 @@ struct XTLaunch {
     const size_t sm = xt_smem<T>(L, B);
     cudaFuncSetAttribute(k_fft_x_tensor<T, L, B, NEXT>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    const NextLin nl = next ? *next : NextLin{};
+    NextLin nl = next ? *next : NextLin{};
+    if (!next) nl.skip_pos = c->skip_pos;
     k_fft_x_tensor<T, L, B, NEXT><<<dim3((g.mz + B - 1) / B, g.ny, 1), L / 4 * B, sm,
                                      c->stream>>>(s03, s45, g.M, y, out, c->rs, g,
                                                   tab<T>(c->tw_x), nl, outsc);
@@ -1933,7 +1973,8 @@ int fft_x_tensor(Ctx *c, const C2<T> *s03, const C2<T> *s45, T *y, T *out, doubl
   prof_begin(c, KK_X_TENSOR);
   IH_TRY(dispatch_len(g.nx, XTLaunch<T>{c, s03, s45, y, out, outsc, next}, allow512<T>()));
   prof_end(c, KK_X_TENSOR,
-           6.0 * g.M * sizeof(C2<T>) + (8.0 + (next ? 4.0 * (next->n + 2) : 0.0)) * g.Next * sizeof(T));
+           6.0 * g.M * sizeof(C2<T>) +
+               ((c->skip_pos ? 6.0 : 8.0) + (next ? 4.0 * (next->n + 2) : 0.0)) * g.Next * sizeof(T));
   return check_launch(c, "k_fft_x_tensor");
 }
 
@@ -2158,14 +2199,44 @@ static int autotune_t(Ctx *c) {
     }
   }
   if (st == IH_OK) c->tensor_fused = best_t;
+  // the y and x passes of the six tensor sources: whole arrays or kz slabs
+  // (with the separate last x pass only; the fused one takes the x pass)
+  c->gw_slab = 0;
+  if (st == IH_OK && !c->tensor_fused) {
+    static const int widths[4] = {0, 8, 16, 32};
+    float tb = 0.f;
+    for (int i = 0; i < 4 && st == IH_OK; ++i) {
+      if (widths[i] >= g.mz) continue;
+      float ms = 0.f;
+      for (int r = 0; r <= reps && st == IH_OK; ++r) {
+        if (r == 1) cudaEventRecord(e0, c->stream);
+        st = fft_gw_yx<T>(c, sp, widths[i]);
+      }
+      if (st != IH_OK) break;
+      cudaEventRecord(e1, c->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        c->err = "autotune: event timing failed";
+        st = IH_ERR_CUDA;
+        break;
+      }
+      ms /= reps;
+      snprintf(line, sizeof line, "gw-yx slab %d %.1f us; ", widths[i], 1e3 * ms);
+      rep += line;
+      if (i == 0 || ms < tb) {
+        c->gw_slab = widths[i];
+        tb = ms;
+      }
+    }
+  }
   c->prof_on = prof;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st != IH_OK) return st;
-  snprintf(line, sizeof line, "chosen: x %s, y %s, deriv4-x %s, rt-x %s, rt-y %s, tensor %s",
+  snprintf(line, sizeof line,
+           "chosen: x %s, y %s, deriv4-x %s, rt-x %s, rt-y %s, tensor %s, gw-yx slab %d",
            variant_name(c->xy_var[0]), variant_name(c->xy_var[1]), variant_name(c->d4_var),
            variant_name(c->rt_var[0]), variant_name(c->rt_var[1]),
-           c->tensor_fused ? "fused" : "separate");
+           c->tensor_fused ? "fused" : "separate", c->gw_slab);
   c->tune_report = rep + line;
   return IH_OK;
 }
@@ -2180,6 +2251,7 @@ int fft_autotune(Ctx *c) {
   template int fft_zr2c<T>(Ctx *, const T *, long long, C2<T> *, long long, int);               \
   template int fft_zc2r<T>(Ctx *, const C2<T> *, long long, T *, long long, int);               \
   template int fft_xy<T>(Ctx *, C2<T> *, long long, int, int, int);                             \
+  template int fft_gw_yx<T>(Ctx *, C2<T> *, int);                                              \
   template int fft_x_deriv4_inv<T>(Ctx *, const C2<T> *, C2<T> *, long long);                   \
   template int fft_z_rhs_fused<T>(Ctx *, const C2<T> *, const T *, const double *, T *, T *,    \
                                   T *, C2<T> *, int, double *, int *, int);                     \

@@ -91,6 +91,10 @@ struct NextLin {
   const void *base;               // the step's start state (T[Nf])
   const double *basesc;
   const double *dt;               // the step size (device memory)
+  // 1: the position derivatives phi' = dphi, psi' = dpsi, h' = dh (copies of
+  // the velocity input) are not written -- stage vectors whose position
+  // halves nothing reads (the velocity form); with or without the above
+  int skip_pos;
 };
 
 // kernel kinds for per-kernel timing and algorithmic-byte accounting
@@ -212,8 +216,10 @@ struct Ctx {
   int roundtrip = 1;  // RHS without filter/output: round trips instead of full spectra
   int tensor_fused = 0;  // update_h fused into the last x pass (autotuner's choice)
   int zwide = 1;         // the wide-row fused z pass where it applies (nz = 256, mixed)
+  int gw_slab = 0;       // kz slab width of the tensor sources' y/x passes (0: whole arrays)
   int stage_fusion = 0;  // DOPRI853 stage inputs formed by the RHS of the previous stage
   int velocity_form = 1; // mixed form: stage combinations from the velocity halves only
+  int skip_pos = 0;      // set during the stage evaluations of a velocity-form try
   std::string tune_report;
 };
 
@@ -262,6 +268,10 @@ int fft_zc2r(Ctx *c, const C2<T> *in, long long in_stride, T *out,
 template <typename T>
 int fft_xy(Ctx *c, C2<T> *data, long long stride, int count, int axis,
            int sign);
+// forward y then x passes of the six tensor sources (spec arrays 0..3, 5, 6),
+// in kz slabs of width w (0: whole arrays)
+template <typename T>
+int fft_gw_yx(Ctx *c, C2<T> *spec, int w);
 // Inverse x-pass that generates the four derivative spectra from phi-hat:
 // out[a] = F_a(k) * phihat(k) / N, a = d/dx, d/dy, d/dz, laplacian, then the
 // inverse x transform of each; phihat is only read.
@@ -309,7 +319,7 @@ int fft_autotune(Ctx *c);
 // the last forward x pass of the six S_ij spectra + update_h (either form);
 // next: also form the tensor segments of the next stage input (in y)
 int tensor_last_pass(Ctx *c, void *spec, void *y, void *out, double *outsc,
-                     const NextLin *next);
+                     const NextLin *next, bool x_done = false);
 int rhs(Ctx *c, double t, Vec &y, Vec &k, int filter, int output,
         const Vec *smry_src, const NextLin *next = nullptr);
 int reduce_mean(Ctx *c, const void *arr, long long n, double *dev_out);

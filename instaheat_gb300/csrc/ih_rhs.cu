@@ -259,9 +259,11 @@ __global__ void k_update_phi_psi(T *y, const double *ysc, const T *__restrict__ 
         o3[w] = (T)0.5 * pp[w] + ps[w] * pm - (T)4.0 * H * dps[w];
       }
     }
-    st_w<T>(out + i0, dph);
+    if (!nl.skip_pos) {
+      st_w<T>(out + i0, dph);
+      st_w<T>(out + 2 * N + i0, dps);
+    }
     st_w<T>(out + N + i0, o1);
-    st_w<T>(out + 2 * N + i0, dps);
     st_w<T>(out + 3 * N + i0, o3);
     if constexpr (NEXT) {
 #pragma unroll
@@ -309,7 +311,7 @@ __global__ void k_next_sc(const NextLin nl, const double *ksc, double *outsc) {
 // six S_ij spectra, spectra 4 and 5 at s + 5M.
 // NEXT: also the next stage's input at the tensor entries of y (nl).
 template <typename T, bool NEXT>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (NEXT ? 3 : 5) : 2)) k_update_h(
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (NEXT ? 3 : 4) : 2)) k_update_h(
     const C2<T> *__restrict__ s, T *y, T *__restrict__ out, const RhsScalars *rs, Geom g,
     const NextLin nl, double *outsc) {
   const long long M = g.M;
@@ -354,30 +356,35 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (NEXT ? 3 : 5) : 2)) k_
 // stage input too (in y).
 template <typename T>
 static int tensor_last_pass_t(Ctx *c, C2<T> *s, T *y, T *out, double *outsc,
-                              const NextLin *next) {
+                              const NextLin *next, bool x_done) {
   const Geom &g = c->g;
   const long long M = g.M;
-  if (c->tensor_fused && g.pow2) return fft_x_tensor<T>(c, s, s + 5 * M, y, out, outsc, next);
-  IH_TRY((fft_xy<T>(c, s, M, 4, 0, -1)));
-  IH_TRY((fft_xy<T>(c, s + 5 * M, M, 2, 0, -1)));
+  if (!x_done) {
+    if (c->tensor_fused && g.pow2) return fft_x_tensor<T>(c, s, s + 5 * M, y, out, outsc, next);
+    IH_TRY((fft_xy<T>(c, s, M, 4, 0, -1)));
+    IH_TRY((fft_xy<T>(c, s + 5 * M, M, 2, 0, -1)));
+  }
   const unsigned gm = grid_for(M, 256, 4);
   prof_begin(c, KK_UPDATE_H);
   if (next) {
     k_update_h<T, true><<<gm, 256, 0, c->stream>>>(s, y, out, c->rs, g, *next, outsc);
   } else {
     NextLin none{};
+    none.skip_pos = c->skip_pos;
     k_update_h<T, false><<<gm, 256, 0, c->stream>>>(s, y, out, c->rs, g, none, outsc);
   }
   prof_end(c, KK_UPDATE_H,
-           6.0 * M * sizeof(C2<T>) + (8.0 + (next ? 4.0 * (next->n + 2) : 0.0)) * g.Next * sizeof(T));
+           6.0 * M * sizeof(C2<T>) +
+               ((c->skip_pos ? 6.0 : 8.0) + (next ? 4.0 * (next->n + 2) : 0.0)) * g.Next * sizeof(T));
   return check_launch(c, "k_update_h");
 }
 int tensor_last_pass(Ctx *c, void *spec, void *y, void *out, double *outsc,
-                     const NextLin *next) {
+                     const NextLin *next, bool x_done) {
   if (c->mixed)
-    return tensor_last_pass_t<float>(c, (C2<float> *)spec, (float *)y, (float *)out, outsc, next);
+    return tensor_last_pass_t<float>(c, (C2<float> *)spec, (float *)y, (float *)out, outsc, next,
+                                     x_done);
   return tensor_last_pass_t<double>(c, (C2<double> *)spec, (double *)y, (double *)out, outsc,
-                                    next);
+                                    next, x_done);
 }
 
 // ---------------------------------------------------------------------------
@@ -1007,14 +1014,21 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
   // 5. tensor modes
   if (c->p.enable_gw) {
     // S_ij spectra: spec[0..3] and spec[5..6]; forward y and x passes
-    // (batched: per-array y-then-x ordering measured slower, no L2 reuse)
-    IH_TRY((fft_xy<T>(c, spec, M, 4, 1, -1)));
-    IH_TRY((fft_xy<T>(c, spec + 5 * M, M, 2, 1, -1)));
-    IH_TRY(tensor_last_pass(c, spec, yfl, kfl, k.sc, next));
+    // (batched: per-array y-then-x ordering measured slower, no L2 reuse;
+    // kz slabs of all six arrays where the autotuner chose them)
+    if (c->gw_slab > 0 && !c->tensor_fused && g.pow2) {
+      IH_TRY((fft_gw_yx<T>(c, spec, c->gw_slab)));
+      IH_TRY(tensor_last_pass(c, spec, yfl, kfl, k.sc, next, true));
+    } else {
+      IH_TRY((fft_xy<T>(c, spec, M, 4, 1, -1)));
+      IH_TRY((fft_xy<T>(c, spec + 5 * M, M, 2, 1, -1)));
+      IH_TRY(tensor_last_pass(c, spec, yfl, kfl, k.sc, next));
+    }
   }
   // 6. phi/psi equations of motion (and the next stage input)
   prof_begin(c, KK_UPDATE_PHI_PSI);
-  const NextLin none{};
+  NextLin none{};
+  none.skip_pos = c->skip_pos;
   const NextLin &nl = next ? *next : none;
   const unsigned gu = grid_for(N / VecW<T>::W, 256, 4);
   if (c->mixed) {
@@ -1032,7 +1046,8 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
       k_update_phi_psi<T, false, false><<<gu, 256, 0, c->stream>>>(yfl, y.sc, lap, p, kfl, c->rs,
                                                                    N, g.mass, nl);
   }
-  prof_end(c, KK_UPDATE_PHI_PSI, (10.0 + (next ? 4.0 * (next->n + 2) : 0.0)) * N * sizeof(T));
+  prof_end(c, KK_UPDATE_PHI_PSI,
+           ((nl.skip_pos ? 8.0 : 10.0) + (next ? 4.0 * (next->n + 2) : 0.0)) * N * sizeof(T));
   IH_TRY(check_launch(c, "k_update_phi_psi"));
   if (next) {
     k_next_sc<<<1, 32, 0, c->stream>>>(*next, k.sc, y.sc);

@@ -985,6 +985,14 @@ static int try_body(Ctx *c) {
   // (the mixed form combines stages in the velocity form instead)
   const bool vel = c->mixed && c->velocity_form;
   const bool fuse = c->stage_fusion && !c->tensor_fused && !vel;
+  {
+  // the velocity form reads no position half of k_2..k_12: their RHS
+  // evaluations skip those copies (k_1, the FSAL vector, keeps them)
+  struct SkipPos {
+    Ctx *c;
+    ~SkipPos() { c->skip_pos = 0; }
+  } guard{c};
+  c->skip_pos = vel ? 1 : 0;
   for (int s = 1; s < 12; ++s) {  // stage s+1 from stages 1..s
     if (vel) {
       IH_TRY(lincomb_vel(c, s));
@@ -1000,6 +1008,7 @@ static int try_body(Ctx *c) {
     if (fuse_next) stage_terms(c, s + 1, true, nullptr, &nl);
     // the RHS does not depend on t explicitly (toolbox.c:75-88)
     IH_TRY(rhs(c, 0.0, c->ytmp, c->k[s + 1], 0, 0, nullptr, fuse_next ? &nl : nullptr));
+  }
   }
   if (vel) return final_vel(c);
   FinalArgs f;

@@ -220,8 +220,10 @@ __device__ __forceinline__ T tensor_eom(const Geom &g, long long id, C2<T> n0, C
                        tm * h1.y - tc.h3 * d1.y + tc.two_inv_a2 * n0.y);
   const V o4 = mk2c<T>(tm * h2.x - tc.h3 * d2.x + tc.two_inv_a2 * n1.x,
                        tm * h2.y - tc.h3 * d2.y + tc.two_inv_a2 * n1.y);
-  ov[e1] = d1;
-  ov[e2] = d2;
+  if (!nl.skip_pos) {
+    ov[e1] = d1;
+    ov[e2] = d2;
+  }
   ov[e3] = o3;
   ov[e4] = o4;
   if constexpr (NEXT) {

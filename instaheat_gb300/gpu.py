@@ -394,9 +394,10 @@ class Context:
 
     def engines(self):
         """Engines of the x, y, fused x passes, the x, y round trips, the form
-        of the last tensor x pass (0 separate, 1 fused) and of the fused z pass
-        (1 wide rows where they apply, 0 a warp per row)."""
-        return tuple(int(self.L_.ih_fft_get_engine(self.h, p)) for p in range(7))
+        of the last tensor x pass (0 separate, 1 fused), of the fused z pass
+        (1 wide rows where they apply, 0 a warp per row) and the kz slab width
+        of the tensor sources' y/x passes (0 whole arrays)."""
+        return tuple(int(self.L_.ih_fft_get_engine(self.h, p)) for p in range(8))
 
     @classmethod
     def _member(cls, handle, p: Params):

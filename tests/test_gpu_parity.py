@@ -319,6 +319,36 @@ def test_rhs_tensor_pass_forms_f64(gpu_mod, oracle_mod, n, L, fused, filt):
     assert max(errs.values()) < 1e-11, errs
 
 
+@pytest.mark.parametrize("prec", ["f64", "mixed"])
+@pytest.mark.parametrize("engine", [1, 2, 3, 4])
+def test_rhs_gw_slabs_bit_identical(gpu_mod, oracle_mod, prec, engine):
+    """The tensor sources' y and x passes kz slab by kz slab (widths 8, 16,
+    32; the last slab takes the remainder) or on whole arrays: every pencil is
+    transformed by the same tile code, so the RHS is the same to the bit; and
+    within 1e-11 of the oracle in FP64."""
+    n, L = (64, 64, 64), (20.0, 20.0, 20.0)
+    precision = gpu_mod.PREC_F64 if prec == "f64" else gpu_mod.PREC_MIXED
+    ctx = gpu_mod.Context(n=n, L=L, precision=precision)
+    ctx.set_engine(0, engine)
+    ctx.set_engine(1, engine)
+    ctx.set_engine(5, 0)
+    o = oracle_mod.Oracle(n=n, L=L)
+    f = make_state(o, seed=25)
+    rs = []
+    for w in (0, 8, 16, 32):
+        ctx.set_engine(7, w)
+        assert ctx.engines()[7] == w
+        rs.append(ctx.mk_rhs(f, filter=0)[0])
+    for r in rs[1:]:
+        assert np.array_equal(r, rs[0])
+    if prec == "f64":
+        r_ref, _ = o.rhs(f, filter=0)
+        errs = seg_rel_err(rs[2], r_ref, o.N, o.Next)
+        assert max(errs.values()) < 1e-11, errs
+    with pytest.raises(RuntimeError):
+        ctx.set_engine(7, 12)
+
+
 def test_rhs_tensor_pass_forms_mixed_agree(gpu_mod, oracle_mod):
     """Mixed form (FP32 transforms): both tensor x-pass forms agree within
     FP32 rounding, 1e-5 of each tensor segment's magnitude."""
@@ -414,7 +444,8 @@ def test_autotune_picks_an_engine_and_keeps_parity(gpu_mod, oracle_mod):
     ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
     rep = ctx.autotune()
     assert "chosen:" in rep
-    assert all(e in ENGINES for e in ctx.engines())
+    assert all(e in ENGINES for e in ctx.engines()[:7])
+    assert ctx.engines()[7] in (0, 8, 16, 32)
     o = oracle_mod.Oracle(n=n)
     f = make_state(o, seed=4)
     r_ref, _ = o.rhs(f, filter=0)
