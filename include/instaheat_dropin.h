@@ -18,7 +18,11 @@
  * third, IH_OUTPUT_INTERVAL (> 0), makes run_dopri853 land steps on
  * ti + k * IH_OUTPUT_INTERVAL and write the time slices there (as its
  * overshoot clamp lands the last step on tf) instead of every
- * TIME_STEP_SKIPS steps.
+ * TIME_STEP_SKIPS steps; with a fourth, IH_DENSE_OUTPUT (1), the steps keep
+ * the controller's size and each slice at ti + k * IH_OUTPUT_INTERVAL < tf
+ * comes from the DOP853 continuous extension of the accepted step that
+ * contains it (ih_dopri853_dense: three extra RHS evaluations per step with
+ * slices, then the output RHS of the interpolated state).
  *
  * Differences from the reference functions, all on the side of what callers
  * observe after a call:

@@ -281,6 +281,29 @@ int ih_dopri853_counters(const ih_context *c, double *dt_next, long *n_ok,
  * b[12], bhh[3] (stages 1, 9, 12), er[12]. */
 int ih_dopri853_tableau(double *c, double *a, double *b, double *bhh,
                         double *er);
+/* Dense-output coefficients of the same method (dopri853_constants.c:23-25,
+ * 98-173, declared but never used by the reference's stepper):
+ * ad[3*16] = the inputs of stages 14..16 over stages 1..16 (stage 13 =
+ * f(field_new)), d[4*16] = the weights d4..d7 over stages 1..16. */
+int ih_dopri853_dense_tableau(double *ad, double *d);
+/* Dense output (no reference counterpart; the reference lands output times
+ * by shortening steps, as IH_OUTPUT_INTERVAL does in the drop-in): the
+ * DOP853 continuous extension (order 7) of the last accepted
+ * ih_dopri853_step at t_out in [t - dt_did, t].  The first call after a step
+ * evaluates stages 14..16 (three RHS evaluations); further calls within the
+ * same step reuse them.  The interpolant runs from the step's start state to
+ * field_new as the post-step RHS left it (filtered in place when the filter
+ * is on, so with the filter it reproduces the filtered end state at t).  With
+ * want_output = 1 the interpolated state then passes through the output RHS
+ * of a saved slice (filtered, diagnostics kept for ih_get_output, summaries
+ * of the interpolated state).  field_out (Ntot doubles, reference layout; may
+ * be NULL) receives the interpolated state, after that RHS when want_output.
+ * The context's own state, time and controller are unchanged.
+ * IH_ERR_STATE without an accepted step since the last state change (a new
+ * try, RK4 step, state upload or standalone RHS ends it); IH_ERR_ARG for
+ * t_out outside the step.  Mixed form: stages 6..12 of a velocity-form step
+ * get their position halves restored from the velocity halves first. */
+int ih_dopri853_dense(ih_context *c, double t_out, int want_output, double *field_out);
 
 /* ---- learned step-size proposer (no reference counterpart) ----
  * A 12 -> 64 -> 64 -> 1 MLP (GELU), BF16 weights, FP32 accumulation, trained

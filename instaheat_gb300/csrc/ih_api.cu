@@ -223,6 +223,8 @@ static void destroy(Ctx *c) {
   free_vec(c->ynew);
   free_vec(c->ytmp);
   for (int j = 0; j < 13; ++j) free_vec(c->k[j]);
+  for (int j = 0; j < 3; ++j) free_vec(c->kd[j]);
+  free_vec(c->dense);
   for (auto &t : c->timers)
     for (auto e : t.ev) cudaEventDestroy(e);
   for (auto e : c->tev)
@@ -320,6 +322,7 @@ int ih_set_state(ih_context *h, const double *f, double t) {
   c->t = t;
   c->have_state = 1;
   c->step_start_valid = 0;
+  c->dense_ready = 0;
   IH_CUDA(c, cudaStreamSynchronize(c->stream));
   return IH_OK;
 }
@@ -369,6 +372,7 @@ int ih_mk_rhs_dev(ih_context *h, double t, double *f_dev, double *result_dev, in
   Ctx *c = &h->c;
   IH_TRY(vec_from_ref(c, f_dev, c->ytmp));
   c->step_start_valid = 0;
+  c->dense_ready = 0;
   IH_TRY(rhs(c, t, c->ytmp, c->ynew, filter, output, nullptr));
   if (filter == 1 && c->p.enable_filter) IH_TRY(vec_to_ref(c, c->ytmp, f_dev));
   const Geom &g = c->g;
@@ -394,6 +398,7 @@ int ih_mk_rhs_host(ih_context *h, double t, double *f, double *result, int filte
   IH_TRY(upload_ref(c, f));
   IH_TRY(vec_from_ref(c, (const double *)c->stage_dev, c->ytmp));
   c->step_start_valid = 0;
+  c->dense_ready = 0;
   IH_TRY(rhs(c, t, c->ytmp, c->ynew, filter, output, nullptr));
   if (filter == 1 && c->p.enable_filter) {
     IH_TRY(vec_to_ref(c, c->ytmp, (double *)c->stage_dev));
@@ -684,6 +689,23 @@ int ih_dopri853_counters(const ih_context *h, double *dt_next, long *n_ok, long 
 
 int ih_dopri853_tableau(double *cc, double *a, double *b, double *bhh, double *er) {
   dopri_tableau(cc, a, b, bhh, er);
+  return IH_OK;
+}
+
+int ih_dopri853_dense_tableau(double *ad, double *d) {
+  dopri_dense_tableau(ad, d);
+  return IH_OK;
+}
+
+int ih_dopri853_dense(ih_context *h, double t_out, int want_output, double *field_out) {
+  CTX_CHECK(h);
+  Ctx *c = &h->c;
+  IH_TRY(dopri_dense(c, t_out, want_output ? 1 : 0));
+  if (field_out) {
+    IH_TRY(vec_to_ref(c, c->dense, (double *)c->stage_dev));
+    IH_TRY(download_ref(c, field_out));
+  }
+  IH_CUDA(c, cudaStreamSynchronize(c->stream));
   return IH_OK;
 }
 

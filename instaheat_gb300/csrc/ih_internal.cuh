@@ -166,6 +166,12 @@ struct Ctx {
 
   // state and stepper vectors
   Vec y, ynew, ytmp, k[13];     // k[1..12] stage RHS, k[1] = dfield
+  Vec kd[3], dense;             // dense output: stages 14..16, the interpolated state
+  int dense_ready = 0;          // the last accepted DOPRI853 step's stages are intact
+  int dense_stages = 0;         // stages 14..16 of that step are evaluated
+  int dense_vel = 0;            // that step combined its stages in the velocity form
+  int try_vel = 0;              // the form of the last try
+  double dense_t0 = 0.0, dense_h = 0.0;  // that step's start and size
   int step_start_valid = 0;     // ynew holds the state at the start of the last step
   double t = 0.0;
   int have_state = 0, dopri_ready = 0;
@@ -356,6 +362,8 @@ int step_accept(Ctx *c, double dt, double err, double rho_mean, int want_output,
 int dopri_step(Ctx *c, double dt_try, int want_output, ih_step_info *info);
 int rk4_step(Ctx *c, double dt, int want_output);
 void dopri_tableau(double *cc, double *a, double *b, double *bhh, double *er);
+void dopri_dense_tableau(double *ad, double *d);
+int dopri_dense(Ctx *c, double t_out, int want_output);
 
 // launch geometry helper: blocks for n items with `per` items per thread
 inline unsigned grid_for(long long n, int threads, int per = 1) {

@@ -37,6 +37,11 @@ static const double DC[12] = {0.0,
                               0.6e+00,
                               0.857142857142857142857142857142e+00,
                               1.0};
+// Dense output (the same authors' continuous extension; the reference
+// declares these in src/dopri853_constants.c:23-25, 98-173 and never uses
+// them): DAD[r] = the input of stage 14 + r over stages 1..16 (stage 13 =
+// f(field_new)), DDN[i] = the weights d(4+i) over stages 1..16.
+static double DAD[3][16], DDN[4][16];
 static int tableau_ready = 0;
 
 static void tableau_init() {
@@ -114,7 +119,89 @@ static void tableau_init() {
   DE3[9] = 0.3341791187130174790297318841e+00;
   DE3[10] = 0.8192320648511571246570742613e-01;
   DE3[11] = -0.2235530786388629525884427845e-01;
+  memset(DAD, 0, sizeof DAD);
+  memset(DDN, 0, sizeof DDN);
+  double(*AD)[16] = DAD;
+  double(*DD)[16] = DDN;
+  AD[0][0] = 5.61675022830479523392909219681e-2;
+  AD[0][6] = 2.53500210216624811088794765333e-1;
+  AD[0][7] = -2.46239037470802489917441475441e-1;
+  AD[0][8] = -1.24191423263816360469010140626e-1;
+  AD[0][9] = 1.5329179827876569731206322685e-1;
+  AD[0][10] = 8.20105229563468988491666602057e-3;
+  AD[0][11] = 7.56789766054569976138603589584e-3;
+  AD[0][12] = -8.298e-3;
+  AD[1][0] = 3.18346481635021405060768473261e-2;
+  AD[1][5] = 2.83009096723667755288322961402e-2;
+  AD[1][6] = 5.35419883074385676223797384372e-2;
+  AD[1][7] = -5.49237485713909884646569340306e-2;
+  AD[1][10] = -1.08347328697249322858509316994e-4;
+  AD[1][11] = 3.82571090835658412954920192323e-4;
+  AD[1][12] = -3.40465008687404560802977114492e-4;
+  AD[1][13] = 1.41312443674632500278074618366e-1;
+  AD[2][0] = -4.28896301583791923408573538692e-1;
+  AD[2][5] = -4.69762141536116384314449447206e0;
+  AD[2][6] = 7.68342119606259904184240953878e0;
+  AD[2][7] = 4.06898981839711007970213554331e0;
+  AD[2][8] = 3.56727187455281109270669543021e-1;
+  AD[2][12] = -1.39902416515901462129418009734e-3;
+  AD[2][13] = 2.9475147891527723389556272149e0;
+  AD[2][14] = -9.15095847217987001081870187138e0;
+  DD[0][0] = -0.84289382761090128651353491142e+01;
+  DD[0][5] = 0.56671495351937776962531783590e+00;
+  DD[0][6] = -0.30689499459498916912797304727e+01;
+  DD[0][7] = 0.23846676565120698287728149680e+01;
+  DD[0][8] = 0.21170345824450282767155149946e+01;
+  DD[0][9] = -0.87139158377797299206789907490e+00;
+  DD[0][10] = 0.22404374302607882758541771650e+01;
+  DD[0][11] = 0.63157877876946881815570249290e+00;
+  DD[0][12] = -0.88990336451333310820698117400e-01;
+  DD[0][13] = 0.18148505520854727256656404962e+02;
+  DD[0][14] = -0.91946323924783554000451984436e+01;
+  DD[0][15] = -0.44360363875948939664310572000e+01;
+  DD[1][0] = 0.10427508642579134603413151009e+02;
+  DD[1][5] = 0.24228349177525818288430175319e+03;
+  DD[1][6] = 0.16520045171727028198505394887e+03;
+  DD[1][7] = -0.37454675472269020279518312152e+03;
+  DD[1][8] = -0.22113666853125306036270938578e+02;
+  DD[1][9] = 0.77334326684722638389603898808e+01;
+  DD[1][10] = -0.30674084731089398182061213626e+02;
+  DD[1][11] = -0.93321305264302278729567221706e+01;
+  DD[1][12] = 0.15697238121770843886131091075e+02;
+  DD[1][13] = -0.31139403219565177677282850411e+02;
+  DD[1][14] = -0.93529243588444783865713862664e+01;
+  DD[1][15] = 0.35816841486394083752465898540e+02;
+  DD[2][0] = 0.19985053242002433820987653617e+02;
+  DD[2][5] = -0.38703730874935176555105901742e+03;
+  DD[2][6] = -0.18917813819516756882830838328e+03;
+  DD[2][7] = 0.52780815920542364900561016686e+03;
+  DD[2][8] = -0.11573902539959630126141871134e+02;
+  DD[2][9] = 0.68812326946963000169666922661e+01;
+  DD[2][10] = -0.10006050966910838403183860980e+01;
+  DD[2][11] = 0.77771377980534432092869265740e+00;
+  DD[2][12] = -0.27782057523535084065932004339e+01;
+  DD[2][13] = -0.60196695231264120758267380846e+02;
+  DD[2][14] = 0.84320405506677161018159903784e+02;
+  DD[2][15] = 0.11992291136182789328035130030e+02;
+  DD[3][0] = -0.25693933462703749003312586129e+02;
+  DD[3][5] = -0.15418974869023643374053993627e+03;
+  DD[3][6] = -0.23152937917604549567536039109e+03;
+  DD[3][7] = 0.35763911791061412378285349910e+03;
+  DD[3][8] = 0.93405324183624310003907691704e+02;
+  DD[3][9] = -0.37458323136451633156875139351e+02;
+  DD[3][10] = 0.10409964950896230045147246184e+03;
+  DD[3][11] = 0.29840293426660503123344363579e+02;
+  DD[3][12] = -0.43533456590011143754432175058e+02;
+  DD[3][13] = 0.96324553959188282948394950600e+02;
+  DD[3][14] = -0.39177261675615439165231486172e+02;
+  DD[3][15] = -0.14972683625798562581422125276e+03;
   tableau_ready = 1;
+}
+
+void dopri_dense_tableau(double *ad, double *d) {
+  tableau_init();
+  if (ad) memcpy(ad, DAD, sizeof DAD);
+  if (d) memcpy(d, DDN, sizeof DDN);
 }
 
 void dopri_tableau(double *cc, double *a, double *b, double *bhh, double *er) {
@@ -493,6 +580,34 @@ struct VelLin {
   const double *dt;
 };
 
+// position half of a velocity-form stage vector, k_j^p = Y_j^v, from the
+// velocity halves its stage input was formed from (the accumulation of
+// k_lincomb_vel), for the dense output, which reads whole stage vectors
+__global__ void k_restore_pos(const float *__restrict__ y, float *__restrict__ kout,
+                              const VelLin a, float dt, long long N, long long Next) {
+  const long long nq = (2 * N + 2 * Next) / 4;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nq;
+       v += (long long)gridDim.x * blockDim.x) {
+    long long ip, iv;
+    int c0, c1;
+    vel_pair(v * 4, N, Next, ip, iv, c0, c1);
+    float av[4] = {0.f, 0.f, 0.f, 0.f}, x[4];
+#pragma unroll
+    for (int j = 0; j < kMaxTerms; ++j) {
+      if (j < a.n) {
+        vload<float>((const float *)a.k[j] + iv, x);
+#pragma unroll
+        for (int w = 0; w < 4; ++w) av[w] += a.cvf[j] * x[w];
+      }
+    }
+    float yv[4], ov[4];
+    vload<float>(y + iv, yv);
+#pragma unroll
+    for (int w = 0; w < 4; ++w) ov[w] = yv[w] + dt * av[w];
+    vstore<float>(kout + ip, ov);
+  }
+}
+
 __global__ void k_lincomb_vel(const float *__restrict__ y, const double *ysc,
                               float *__restrict__ out, double *outsc, const VelLin a, long long N,
                               long long Next) {
@@ -802,6 +917,7 @@ int dopri_init(Ctx *c, const ih_dopri_cfg *cfg, double t0, double dt0, int want_
   c->reject = 0;
   c->n_ok = c->n_bad = c->n_stp = c->n_tries = 0;
   c->hist_n = 0;
+  c->dense_ready = 0;
   // prepare_and_save_timeslice: RHS with the filter on (toolbox.c:96-104)
   IH_TRY(rhs(c, t0, c->y, c->k[1], 1, want_output, nullptr));
   c->dopri_ready = 1;
@@ -858,16 +974,17 @@ static void vel_tables() {
   });
 }
 
-// the input of stage s+1 in the velocity form (mixed form)
-static int lincomb_vel(Ctx *c, int s) {
+// the terms of the velocity-form input of stage s+1; stage[l] = stage l+1's
+// vector (null: not available, an error if the stage has a term)
+static int vel_terms(int s, const Vec *const stage[12], VelLin &a) {
   vel_tables();
-  VelLin a;
   memset(&a, 0, sizeof a);
   int n = 0;
   for (int l = 0; l < s; ++l) {
     if (DA[s][l] == 0.0 && VAA[s][l] == 0.0) continue;
-    a.k[n] = c->k[l + 1].fl;
-    a.ksc[n] = c->k[l + 1].sc;
+    if (!stage[l]) return IH_ERR_STATE;
+    a.k[n] = stage[l]->fl;
+    a.ksc[n] = stage[l]->sc;
     a.cv[n] = DA[s][l];
     a.cvf[n] = (float)DA[s][l];
     a.cpf[n] = (float)VAA[s][l];
@@ -875,6 +992,16 @@ static int lincomb_vel(Ctx *c, int s) {
   }
   a.n = n;
   a.csf = (float)VCS[s];
+  return IH_OK;
+}
+
+// the input of stage s+1 in the velocity form (mixed form)
+static int lincomb_vel(Ctx *c, int s) {
+  VelLin a;
+  const Vec *stage[12];
+  for (int l = 0; l < 12; ++l) stage[l] = &c->k[l + 1];
+  IH_TRY(vel_terms(s, stage, a));
+  const int n = a.n;
   a.dt = c->dt_dev;
   const Geom &g = c->g;
   const long long nq = (2 * g.N + 2 * g.Next) / 4;
@@ -985,6 +1112,7 @@ static int try_body(Ctx *c) {
   // (the mixed form combines stages in the velocity form instead)
   const bool vel = c->mixed && c->velocity_form;
   const bool fuse = c->stage_fusion && !c->tensor_fused && !vel;
+  c->try_vel = vel ? 1 : 0;
   {
   // the velocity form reads no position half of k_2..k_12: their RHS
   // evaluations skip those copies (k_1, the FSAL vector, keeps them)
@@ -1109,6 +1237,7 @@ static int replay(Ctx *c, int kind, const void *const key[4], Body body) {
 // the try and the read-back of its error on the context stream and returns;
 // try_collect waits for them.
 int try_enqueue(Ctx *c, double dt) {
+  c->dense_ready = 0;  // the try overwrites the stage vectors and ynew
   c->hpin[kDtSlot] = dt;
   IH_CUDA(c, cudaMemcpyAsync(c->dt_dev, c->hpin + kDtSlot, sizeof(double), cudaMemcpyHostToDevice,
                              c->stream));
@@ -1184,6 +1313,11 @@ int step_accept(Ctx *c, double dt, double err, double rho_mean, int want_output,
   tmp = c->k[1];
   c->k[1] = c->k[2];
   c->k[2] = tmp;
+  c->dense_t0 = c->t;
+  c->dense_h = dt;
+  c->dense_ready = 1;
+  c->dense_stages = 0;
+  c->dense_vel = c->try_vel;
   c->t += dt;
   c->step_start_valid = 1;
   // step history; with a proposer its proposal replaces the controller's
@@ -1249,8 +1383,113 @@ int dopri_step(Ctx *c, double dt_try, int want_output, ih_step_info *info) {
   return step_accept(c, dt, err, rho_mean, want_output, tries, info);
 }
 
+// The DOP853 continuous extension of the last accepted step at t_out in
+// [t - dt_did, t] (Hairer, Norsett & Wanner; coefficients
+// dopri853_constants.c:23-25, 98-173).  Ingredients after step_accept: the
+// step's start state in ynew, field_new (after the post-step RHS, filtered
+// in place when the filter is on) in y, stage 1 in k[2], stages 3..12 in
+// k[3..12], stage 13 = f(field_new) in k[1]; stages 14..16 are evaluated
+// once per step into kd[0..2].  The interpolant
+//   r1 + th (r2 + s (r3 + th (r4 + s (r5 + th (r6 + s (r7 + th r8)))))),
+//   s = 1 - th, r1 = y0, r2 = field_new - y0, r3 = h k1 - r2,
+//   r4 = r2 - h k13 - r3, r(5+i) = h sum_j d(4+i)j k_j,
+// is formed as y0 + h sum_j W_j k_j + u (field_new - y0) with u = th^2 (3 - 2
+// th) and W_j = th^2 s^2 d4j + th^3 s^2 d5j + th^3 s^3 d6j + th^4 s^3 d7j
+// (+ th s^2 on k1, - th^2 s on k13).  A velocity-form step has no position
+// halves in stages 6..12; they are restored from the velocity halves first.
+int dopri_dense(Ctx *c, double t_out, int want_output) {
+  if (!c->dense_ready) {
+    c->err = "dense output: no accepted DOPRI853 step since the last state change";
+    return IH_ERR_STATE;
+  }
+  const double h = c->dense_h, t0 = c->dense_t0;
+  double th = (t_out - t0) / h;
+  const double tol = 1e-12;
+  if (!(th >= -tol && th <= 1.0 + tol)) {
+    c->err = "dense output: t_out outside the last accepted step";
+    return IH_ERR_ARG;
+  }
+  th = th < 0.0 ? 0.0 : (th > 1.0 ? 1.0 : th);
+  tableau_init();
+  for (int r = 0; r < 3; ++r) IH_TRY(alloc_vec(c, c->kd[r]));
+  IH_TRY(alloc_vec(c, c->dense));
+  const Vec *st[16] = {&c->k[2], nullptr,   &c->k[3],  &c->k[4],  &c->k[5],  &c->k[6],
+                       &c->k[7], &c->k[8],  &c->k[9],  &c->k[10], &c->k[11], &c->k[12],
+                       &c->k[1], &c->kd[0], &c->kd[1], &c->kd[2]};
+  const Vec &y0 = c->ynew;
+  const Geom &g = c->g;
+  if (!c->dense_stages) {
+    if (c->dense_vel) {  // position halves of stages 6..12
+      const Vec *vst[12];
+      for (int l = 0; l < 12; ++l) vst[l] = st[l];
+      for (int s = 5; s < 12; ++s) {
+        VelLin a;
+        IH_TRY(vel_terms(s, vst, a));
+        const long long nq = (2 * g.N + 2 * g.Next) / 4;
+        prof_begin(c, KK_LINCOMB);
+        k_restore_pos<<<stream_grid(nq), 256, 0, c->stream>>>(
+            (const float *)y0.fl, (float *)c->k[s + 1].fl, a, (float)h, g.N, g.Next);
+        prof_end(c, KK_LINCOMB, (double)(a.n + 2) * (g.Nf / 2) * sizeof(float));
+        IH_TRY(check_launch(c, "k_restore_pos"));
+      }
+    }
+    for (int r = 0; r < 3; ++r) {  // stages 14..16
+      LinArgs a;
+      memset(&a, 0, sizeof a);
+      for (int j = 0; j < 13 + r; ++j) {
+        if (DAD[r][j] == 0.0) continue;
+        if (!st[j] || a.n == kMaxTerms) return IH_ERR_STATE;  // fixed by the tableau
+        a.in[a.n] = st[j]->fl;
+        a.insc[a.n] = st[j]->sc;
+        a.coef[a.n] = DAD[r][j];
+        ++a.n;
+      }
+      a.scale = h;
+      IH_TRY(lincomb(c, y0, c->ytmp, a));
+      IH_TRY(rhs(c, 0.0, c->ytmp, c->kd[r], 0, 0, nullptr, nullptr));
+    }
+    c->dense_stages = 1;
+  }
+  const double s1 = 1.0 - th;
+  const double gq[4] = {th * th * s1 * s1, th * th * th * s1 * s1, th * th * th * s1 * s1 * s1,
+                        th * th * th * th * s1 * s1 * s1};
+  LinArgs a;
+  memset(&a, 0, sizeof a);
+  for (int j = 0; j < 16; ++j) {
+    if (!st[j]) continue;
+    double w = 0.0;
+    for (int i = 0; i < 4; ++i) w += gq[i] * DDN[i][j];
+    if (j == 0) w += th * s1 * s1;
+    if (j == 12) w -= th * th * s1;
+    if (w == 0.0) continue;
+    if (a.n == kMaxTerms) return IH_ERR_STATE;  // 12 weighted stages at most
+    a.in[a.n] = st[j]->fl;
+    a.insc[a.n] = st[j]->sc;
+    a.coef[a.n] = w;
+    ++a.n;
+  }
+  a.scale = h;
+  IH_TRY(lincomb(c, y0, c->ytmp, a));
+  const double u = th * th * (3.0 - 2.0 * th);
+  LinArgs b;
+  memset(&b, 0, sizeof b);
+  b.in[0] = c->y.fl;
+  b.insc[0] = c->y.sc;
+  b.coef[0] = u;
+  b.in[1] = y0.fl;
+  b.insc[1] = y0.sc;
+  b.coef[1] = -u;
+  b.n = 2;
+  b.scale = 1.0;
+  IH_TRY(lincomb(c, c->ytmp, c->dense, b));
+  // the output RHS of a saved slice (filtered, diagnostics kept), on the copy
+  if (want_output) IH_TRY(rhs(c, t_out, c->dense, c->ytmp, 1, 1, nullptr));
+  return IH_OK;
+}
+
 // rk4.c:108-161 (one step)
 int rk4_step(Ctx *c, double dt, int want_output) {
+  c->dense_ready = 0;
   for (int j = 1; j <= 4; ++j) IH_TRY(alloc_vec(c, c->k[j]));
   const double t = c->t;
   IH_TRY(rhs(c, t, c->y, c->k[1], 1, want_output, nullptr));

@@ -257,7 +257,14 @@ void run_dopri853()
     size_t n_stp, n_ok = 0, n_bad = 0;
 #ifdef IH_OUTPUT_INTERVAL
     /* output landing: steps are shortened to end on ti + k * interval, and
-     * the slices are written there instead of every TIME_STEP_SKIPS steps */
+     * the slices are written there instead of every TIME_STEP_SKIPS steps;
+     * with IH_DENSE_OUTPUT (1) the steps keep their size and the slices come
+     * from the continuous extension of the step that contains them */
+#if defined(IH_DENSE_OUTPUT)
+    const int dense = (IH_DENSE_OUTPUT) != 0;
+#else
+    const int dense = 0;
+#endif
     size_t n_out = 1;
     double t_out_next = pars.t.ti + (double)n_out * IH_OUTPUT_INTERVAL;
 #endif
@@ -268,7 +275,7 @@ void run_dopri853()
         }
 #ifdef IH_OUTPUT_INTERVAL
         int out = 0;
-        if (t_out_next < tf && t + dt * 1.0001 > t_out_next) {
+        if (!dense && t_out_next < tf && t + dt * 1.0001 > t_out_next) {
             dt = t_out_next - t;
             out = 1;
         }
@@ -293,6 +300,17 @@ void run_dopri853()
         pars.t.t = t;
         t_out.tmp[0] = t;
 #ifdef IH_OUTPUT_INTERVAL
+        while (dense && t_out_next < tf && t_out_next <= t) {
+            IH_CHECK("run_dopri853", ih_dopri853_dense(c, t_out_next, 1, field));
+            fill_outputs(c);
+            pars.t.t = t_out_next;
+            t_out.tmp[0] = t_out_next;
+            save();
+            ++n_out;
+            t_out_next = pars.t.ti + (double)n_out * IH_OUTPUT_INTERVAL;
+            pars.t.t = t;
+            t_out.tmp[0] = t;
+        }
         /* a rejected landing try ends short of the output time: no slice */
         if (out && fabs(t - t_out_next) <= 1e-12 * fmax(1.0, fabs(t_out_next))) {
             IH_CHECK("run_dopri853", ih_get_state(c, field));

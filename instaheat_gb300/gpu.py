@@ -157,6 +157,8 @@ def load(build_if_missing: bool = True):
     L.ih_rhs_roundtrip.argtypes = [vp, C.c_int]
     L.ih_stage_fusion.argtypes = [vp, C.c_int]
     L.ih_velocity_form.argtypes = [vp, C.c_int]
+    L.ih_dopri853_dense.argtypes = [vp, C.c_double, C.c_int, _dp]
+    L.ih_dopri853_dense_tableau.argtypes = [_dp, _dp]
     L.ih_ensemble_create.argtypes = [C.POINTER(Params), C.c_int, C.POINTER(vp)]
     L.ih_ensemble_destroy.argtypes = [vp]
     L.ih_ensemble_destroy.restype = None
@@ -293,6 +295,14 @@ def tableau():
     c = np.zeros(12); a = np.zeros((12, 12)); b = np.zeros(12); bhh = np.zeros(3); er = np.zeros(12)
     load().ih_dopri853_tableau(_ptr(c), _ptr(a), _ptr(b), _ptr(bhh), _ptr(er))
     return c, a, b, bhh, er
+
+
+def dense_tableau():
+    """(ad[3][16], d[4][16]): the inputs of DOPRI853 stages 14..16 and the
+    dense-output weights d4..d7 over stages 1..16."""
+    ad = np.zeros((3, 16)); d = np.zeros((4, 16))
+    load().ih_dopri853_dense_tableau(_ptr(ad), _ptr(d))
+    return ad, d
 
 
 def dopri_cfg(rtol=1e-10, atol=1e-10, beta=0.0, safe=0.9, minscale=0.333, maxscale=3.0,
@@ -571,6 +581,16 @@ class Context:
         st = self.L_.ih_dopri853_step(self.h, dt_try, int(output), C.byref(info))
         self._ck(st, "ih_dopri853_step")
         return info
+
+    def dopri_dense(self, t_out, output=False):
+        """The DOP853 continuous extension of the last accepted step at t_out
+        (in [t - dt_did, t]); with output=True the interpolated state passes
+        through the output RHS (filtered, diagnostics for get_output).
+        Returns the interpolated state (reference layout)."""
+        f = np.zeros(self.Ntot)
+        self._ck(self.L_.ih_dopri853_dense(self.h, t_out, int(output), _ptr(f)),
+                 "ih_dopri853_dense")
+        return f
 
     def dopri_run(self, tf, max_steps=10 ** 9, log_cap=0):
         log = np.zeros(4 * max(1, log_cap))

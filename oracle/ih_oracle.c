@@ -637,6 +637,11 @@ static const double DP_C[12] = {
 
 static double DP_A[12][12];
 static double DP_B[12], DP_E3[12], DP_BHH[3];
+/* dense output (dopri853_constants.c:23-25, 98-173; declared but unused by
+   the reference's stepper): the inputs of stages 14-16 over stages 1..16
+   (stage 13 = f(field_new)) and the weights d4..d7 of the continuous
+   extension's last four coefficient vectors */
+static double DP_AD[3][16], DP_D[4][16];
 static int dp_ready = 0;
 
 static void dp_init(void)
@@ -715,7 +720,89 @@ static void dp_init(void)
     DP_E3[9] = 0.3341791187130174790297318841e+00;
     DP_E3[10] = 0.8192320648511571246570742613e-01;
     DP_E3[11] = -0.2235530786388629525884427845e-01;
+    memset(DP_AD, 0, sizeof DP_AD);
+    memset(DP_D, 0, sizeof DP_D);
+    double (*AD)[16] = DP_AD, (*DD)[16] = DP_D;
+    AD[0][0] = 5.61675022830479523392909219681e-2;
+    AD[0][6] = 2.53500210216624811088794765333e-1;
+    AD[0][7] = -2.46239037470802489917441475441e-1;
+    AD[0][8] = -1.24191423263816360469010140626e-1;
+    AD[0][9] = 1.5329179827876569731206322685e-1;
+    AD[0][10] = 8.20105229563468988491666602057e-3;
+    AD[0][11] = 7.56789766054569976138603589584e-3;
+    AD[0][12] = -8.298e-3;
+    AD[1][0] = 3.18346481635021405060768473261e-2;
+    AD[1][5] = 2.83009096723667755288322961402e-2;
+    AD[1][6] = 5.35419883074385676223797384372e-2;
+    AD[1][7] = -5.49237485713909884646569340306e-2;
+    AD[1][10] = -1.08347328697249322858509316994e-4;
+    AD[1][11] = 3.82571090835658412954920192323e-4;
+    AD[1][12] = -3.40465008687404560802977114492e-4;
+    AD[1][13] = 1.41312443674632500278074618366e-1;
+    AD[2][0] = -4.28896301583791923408573538692e-1;
+    AD[2][5] = -4.69762141536116384314449447206e0;
+    AD[2][6] = 7.68342119606259904184240953878e0;
+    AD[2][7] = 4.06898981839711007970213554331e0;
+    AD[2][8] = 3.56727187455281109270669543021e-1;
+    AD[2][12] = -1.39902416515901462129418009734e-3;
+    AD[2][13] = 2.9475147891527723389556272149e0;
+    AD[2][14] = -9.15095847217987001081870187138e0;
+    DD[0][0] = -0.84289382761090128651353491142e+01;
+    DD[0][5] = 0.56671495351937776962531783590e+00;
+    DD[0][6] = -0.30689499459498916912797304727e+01;
+    DD[0][7] = 0.23846676565120698287728149680e+01;
+    DD[0][8] = 0.21170345824450282767155149946e+01;
+    DD[0][9] = -0.87139158377797299206789907490e+00;
+    DD[0][10] = 0.22404374302607882758541771650e+01;
+    DD[0][11] = 0.63157877876946881815570249290e+00;
+    DD[0][12] = -0.88990336451333310820698117400e-01;
+    DD[0][13] = 0.18148505520854727256656404962e+02;
+    DD[0][14] = -0.91946323924783554000451984436e+01;
+    DD[0][15] = -0.44360363875948939664310572000e+01;
+    DD[1][0] = 0.10427508642579134603413151009e+02;
+    DD[1][5] = 0.24228349177525818288430175319e+03;
+    DD[1][6] = 0.16520045171727028198505394887e+03;
+    DD[1][7] = -0.37454675472269020279518312152e+03;
+    DD[1][8] = -0.22113666853125306036270938578e+02;
+    DD[1][9] = 0.77334326684722638389603898808e+01;
+    DD[1][10] = -0.30674084731089398182061213626e+02;
+    DD[1][11] = -0.93321305264302278729567221706e+01;
+    DD[1][12] = 0.15697238121770843886131091075e+02;
+    DD[1][13] = -0.31139403219565177677282850411e+02;
+    DD[1][14] = -0.93529243588444783865713862664e+01;
+    DD[1][15] = 0.35816841486394083752465898540e+02;
+    DD[2][0] = 0.19985053242002433820987653617e+02;
+    DD[2][5] = -0.38703730874935176555105901742e+03;
+    DD[2][6] = -0.18917813819516756882830838328e+03;
+    DD[2][7] = 0.52780815920542364900561016686e+03;
+    DD[2][8] = -0.11573902539959630126141871134e+02;
+    DD[2][9] = 0.68812326946963000169666922661e+01;
+    DD[2][10] = -0.10006050966910838403183860980e+01;
+    DD[2][11] = 0.77771377980534432092869265740e+00;
+    DD[2][12] = -0.27782057523535084065932004339e+01;
+    DD[2][13] = -0.60196695231264120758267380846e+02;
+    DD[2][14] = 0.84320405506677161018159903784e+02;
+    DD[2][15] = 0.11992291136182789328035130030e+02;
+    DD[3][0] = -0.25693933462703749003312586129e+02;
+    DD[3][5] = -0.15418974869023643374053993627e+03;
+    DD[3][6] = -0.23152937917604549567536039109e+03;
+    DD[3][7] = 0.35763911791061412378285349910e+03;
+    DD[3][8] = 0.93405324183624310003907691704e+02;
+    DD[3][9] = -0.37458323136451633156875139351e+02;
+    DD[3][10] = 0.10409964950896230045147246184e+03;
+    DD[3][11] = 0.29840293426660503123344363579e+02;
+    DD[3][12] = -0.43533456590011143754432175058e+02;
+    DD[3][13] = 0.96324553959188282948394950600e+02;
+    DD[3][14] = -0.39177261675615439165231486172e+02;
+    DD[3][15] = -0.14972683625798562581422125276e+03;
     dp_ready = 1;
+}
+
+void iho_dopri853_dense_tableau(double *ad, double *d)
+{
+    dp_init();
+    if (ad) memcpy(ad, DP_AD, sizeof DP_AD);
+    if (d) memcpy(d, DP_D, sizeof DP_D);
 }
 
 void iho_dopri853_tableau(double *c, double *a, double *b, double *bhh,
@@ -831,10 +918,61 @@ void iho_dopri853_init(iho_ctx *c, const iho_dopri_cfg *cfg,
     mk_rhs_impl(c, t0, field, dfield, 1, 0, NULL, NULL);
 }
 
-/* dopri853.c:271-311 */
-int iho_dopri853_step(iho_ctx *c, const iho_dopri_cfg *cfg,
-                      iho_dopri_state *st, double *field, double *dfield,
-                      double dt_try, iho_output *out)
+/* The continuous extension of the accepted step (Hairer, Norsett & Wanner,
+   the DOP853 dense output; coefficients dopri853_constants.c:23-25, 98-173):
+   stages 14-16 from y = field, the stages of the try (stage 1 = dfield, 6..10
+   in k6..k10, 11 in k2, 12 in k3) and stage 13 = dfield_new = f(field_new),
+   then per element
+     r1 = y, r2 = field_new - y, r3 = dt k1 - r2, r4 = r2 - dt k13 - r3,
+     r(5+i) = dt sum_j d(4+i)j k_j,
+     y(theta) = r1 + theta (r2 + s (r3 + theta (r4 + s (r5 + theta (r6
+                + s (r7 + theta r8)))))),  s = 1 - theta.
+   field_new is the state after the post-step RHS (filtered in place when the
+   filter is on).  Stages 14-16 go to the buffers of stages 4, 5 and yerr. */
+static void dense_output(iho_ctx *c, const double *field, const double *dfield,
+                         double t, double dt, int n, const double *theta,
+                         double *out)
+{
+    dp_init();
+    const size_t Ntot = c->Ntot;
+    const double *kb[16] = {dfield, NULL, NULL, NULL, NULL, c->k6, c->k7,
+                            c->k8, c->k9, c->k10, c->k2, c->k3,
+                            c->dfield_new, c->k4, c->k5, c->yerr};
+    for (int r = 0; r < 3; ++r) {
+        #pragma omp parallel for
+        for (size_t i = 0; i < Ntot; ++i) {
+            double acc = 0.0;
+            for (int j = 0; j < 13 + r; ++j)
+                if (DP_AD[r][j] != 0.0) acc += DP_AD[r][j] * kb[j][i];
+            c->ktmp[i] = field[i] + dt * acc;
+        }
+        mk_rhs_impl(c, t, c->ktmp, (double *)kb[13 + r], 0, 0, NULL, NULL);
+    }
+    for (int q = 0; q < n; ++q) {
+        const double th = theta[q], s1 = 1.0 - th;
+        double *o = out + (size_t)q * Ntot;
+        #pragma omp parallel for
+        for (size_t i = 0; i < Ntot; ++i) {
+            double d[4];
+            for (int r = 0; r < 4; ++r) {
+                double acc = 0.0;
+                for (int j = 0; j < 16; ++j)
+                    if (DP_D[r][j] != 0.0) acc += DP_D[r][j] * kb[j][i];
+                d[r] = dt * acc;
+            }
+            const double r1 = field[i], r2 = c->field_new[i] - field[i];
+            const double r3 = dt * dfield[i] - r2;
+            const double r4 = r2 - dt * c->dfield_new[i] - r3;
+            o[i] = r1 + th * (r2 + s1 * (r3 + th * (r4 + s1 * (d[0] + th * (d[1] +
+                   s1 * (d[2] + th * d[3]))))));
+        }
+    }
+}
+
+static int dopri853_step_impl(iho_ctx *c, const iho_dopri_cfg *cfg,
+                              iho_dopri_state *st, double *field, double *dfield,
+                              double dt_try, iho_output *out, int n_dense,
+                              const double *theta, double *dense_out)
 {
     double dt = dt_try;
     for (;;) {
@@ -847,10 +985,28 @@ int iho_dopri853_step(iho_ctx *c, const iho_dopri_cfg *cfg,
     }
     mk_rhs_impl(c, st->t + dt, c->field_new, c->dfield_new, 1, out ? 1 : 0, out,
                 field);
+    if (n_dense > 0) dense_output(c, field, dfield, st->t, dt, n_dense, theta, dense_out);
     memcpy(field, c->field_new, sizeof(double) * c->Ntot);
     memcpy(dfield, c->dfield_new, sizeof(double) * c->Ntot);
     st->t += (st->dt_did = dt);
     return 0;
+}
+
+/* dopri853.c:271-311 */
+int iho_dopri853_step(iho_ctx *c, const iho_dopri_cfg *cfg,
+                      iho_dopri_state *st, double *field, double *dfield,
+                      double dt_try, iho_output *out)
+{
+    return dopri853_step_impl(c, cfg, st, field, dfield, dt_try, out, 0, NULL, NULL);
+}
+
+int iho_dopri853_step_dense(iho_ctx *c, const iho_dopri_cfg *cfg,
+                            iho_dopri_state *st, double *field, double *dfield,
+                            double dt_try, int n, const double *theta,
+                            double *dense_out)
+{
+    return dopri853_step_impl(c, cfg, st, field, dfield, dt_try, NULL, n, theta,
+                              dense_out);
 }
 
 /* dopri853.c:112-158 (without I/O) */

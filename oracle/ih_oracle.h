@@ -112,6 +112,10 @@ void iho_dopri853_tableau(double *c, double *a, double *b, double *bhh,
 
 /* Initialise: state->t = t0, dt = dt0; computes dfield = rhs(field) with
  * filter=1 and output=0 like prepare_and_save_timeslice (toolbox.c:96-104). */
+/* the dense-output coefficients (dopri853_constants.c:23-25, 98-173):
+   ad[3][16] = inputs of stages 14..16 over stages 1..16 (stage 13 =
+   f(field_new)), d[4][16] = d4..d7 over stages 1..16 */
+void iho_dopri853_dense_tableau(double *ad, double *d);
 void iho_dopri853_init(iho_ctx *c, const iho_dopri_cfg *cfg,
                        iho_dopri_state *st, double *field, double *dfield,
                        double t0, double dt0);
@@ -121,6 +125,14 @@ void iho_dopri853_init(iho_ctx *c, const iho_dopri_cfg *cfg,
 int iho_dopri853_step(iho_ctx *c, const iho_dopri_cfg *cfg,
                       iho_dopri_state *st, double *field, double *dfield,
                       double dt_try, iho_output *out);
+/* iho_dopri853_step (no output flag), then the DOP853 continuous extension
+   of the accepted step at the n fractions theta[q] of it (0 = the step's
+   start, 1 = its end): dense_out[q * Ntot + i].  Three extra RHS
+   evaluations (stages 14-16). */
+int iho_dopri853_step_dense(iho_ctx *c, const iho_dopri_cfg *cfg,
+                            iho_dopri_state *st, double *field, double *dfield,
+                            double dt_try, int n, const double *theta,
+                            double *dense_out);
 /* run loop (dopri853.c:112-158) from st->t to tf, capped at max_steps; the
  * step log (t, dt_did, err, accepted) is written to log[4*k] when log is not
  * NULL and k < log_cap.  Returns number of accepted steps. */

@@ -96,6 +96,10 @@ def lib():
         L.iho_variance.restype = C.c_double
         L.iho_variance.argtypes = [C.c_double, _dp, C.c_size_t]
         L.iho_dopri853_tableau.argtypes = [_dp] * 5
+        L.iho_dopri853_dense_tableau.argtypes = [_dp] * 2
+        L.iho_dopri853_step_dense.restype = C.c_int
+        L.iho_dopri853_step_dense.argtypes = [C.c_void_p, C.POINTER(DopriCfg), C.POINTER(DopriState),
+                                              _dp, _dp, C.c_double, C.c_int, _dp, _dp]
         L.iho_dopri853_init.argtypes = [C.c_void_p, C.POINTER(DopriCfg), C.POINTER(DopriState),
                                         _dp, _dp, C.c_double, C.c_double]
         L.iho_dopri853_step.restype = C.c_int
@@ -126,6 +130,15 @@ def tableau():
     c = np.zeros(12); a = np.zeros((12, 12)); b = np.zeros(12); bhh = np.zeros(3); er = np.zeros(12)
     lib().iho_dopri853_tableau(ptr(c), ptr(a), ptr(b), ptr(bhh), ptr(er))
     return c, a, b, bhh, er
+
+
+def dense_tableau():
+    """(ad[3][16], d[4][16]): the inputs of DOPRI853 stages 14..16 and the
+    dense-output weights d4..d7, over stages 1..16 (dopri853_constants.c:23-25,
+    98-173)."""
+    ad = np.zeros((3, 16)); d = np.zeros((4, 16))
+    lib().iho_dopri853_dense_tableau(ptr(ad), ptr(d))
+    return ad, d
 
 
 class DiagOutput:
@@ -250,6 +263,15 @@ class Oracle:
     def dopri_step(self, field, dfield, cfg, st, dt_try, diag: DiagOutput | None = None):
         return lib().iho_dopri853_step(self.ctx, C.byref(cfg), C.byref(st), ptr(field), ptr(dfield),
                                        dt_try, C.byref(diag.s) if diag is not None else None)
+
+    def dopri_step_dense(self, field, dfield, cfg, st, dt_try, theta):
+        """One DOPRI853 step, then the continuous extension of the accepted
+        step at the fractions theta of it: returns (status, array [len, Ntot])."""
+        th = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).ravel())
+        out = np.zeros((len(th), self.Ntot))
+        rc = lib().iho_dopri853_step_dense(self.ctx, C.byref(cfg), C.byref(st), ptr(field),
+                                           ptr(dfield), dt_try, len(th), ptr(th), ptr(out))
+        return rc, out
 
     def dopri_run(self, field, dfield, cfg, st, tf, max_steps, log_cap=0):
         log = np.zeros(4 * max(log_cap, 1))

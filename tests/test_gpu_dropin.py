@@ -211,3 +211,68 @@ def test_run_dopri853_output_landing(tmp_path, oracle_mod):
     # so the wrap-up adds no slice at 0.05 (dopri853.c:209-212)
     np.testing.assert_allclose(times, [0.0, 0.02, 0.04], atol=1e-14)
     _compare_series(got, exp)
+
+
+def _expected_dense(oracle_mod, p):
+    """run_dopri853 with dense output (IH_OUTPUT_INTERVAL + IH_DENSE_OUTPUT)
+    restated over the oracle: the controller's steps; a step that contains
+    output times is redone from its start with the oracle's continuous
+    extension at those times, whose states pass through the output RHS."""
+    n = (int(p["GRIDPOINTS_X"]),) * 3
+    o = oracle_mod.Oracle(n=n, bins=int(p["POWER_SPECTRUM_BINS"]))
+    f = _initial_state(o)
+    o.initial_psi(f)
+    cfg = oracle_mod.default_cfg(float(p["RELATIVE_TOLERANCE"]), float(p["ABSOLUTE_TOLERANCE"]),
+                                 float(p["MAX_DT_HUBBLE_FRACTION"]))
+    tf, dt = float(p["FINAL_TIME"]), float(p["DELTA_T"])
+    interval = float(p["IH_OUTPUT_INTERVAL"])
+    out = {}
+    d = oracle_mod.DiagOutput(o.bins)
+    _, f_filt = o.rhs(f, filter=1, output=1, diag=d)
+    _record(out, o, f_filt, 0.0, d, o.field_array("rho"))
+    st, df = o.dopri_init(f, cfg, 0.0, dt)
+    t, n_out = 0.0, 1
+    t_next = n_out * interval
+    dense_steps = 0
+    while True:
+        if t + dt * 1.0001 > tf:
+            dt = tf - t
+        f0, df0, st0, t0 = f.copy(), df.copy(), type(st).from_buffer_copy(st), t
+        assert o.dopri_step(f, df, cfg, st, dt) == 0
+        t = st.t
+        times = []
+        while t_next < tf and t_next <= t:
+            times.append(t_next)
+            n_out += 1
+            t_next = n_out * interval
+        if times:
+            h = st.dt_did
+            f[:], df[:] = f0, df0
+            st = type(st).from_buffer_copy(st0)
+            rc, dense = o.dopri_step_dense(f, df, cfg, st, dt, [(x - t0) / h for x in times])
+            assert rc == 0 and st.dt_did == h
+            dense_steps += 1
+            for x, fd in zip(times, dense):
+                d = oracle_mod.DiagOutput(o.bins)
+                _, fd = o.rhs(fd, t=x, filter=1, output=1, diag=d)
+                _record(out, o, fd, x, d, o.field_array("rho"))
+        if t >= tf:
+            break
+        dt = st.dt_next
+    saves = len(out["time"])
+    if saves % int(p["WRITE_OUT_BUFFER_NUMBER"]) != 0 and out["time"][-1][0] < t:
+        d = oracle_mod.DiagOutput(o.bins)
+        _, f = o.rhs(f, t=t, filter=1, output=1, diag=d)
+        _record(out, o, f, t, d, o.field_array("rho"))
+    assert dense_steps >= 1
+    return {k: np.array(v) for k, v in out.items()}
+
+
+def test_run_dopri853_dense_output(tmp_path, oracle_mod):
+    p, got, _ = _run_host(tmp_path, "parameters_dense.sh", oracle_mod)
+    exp = _expected_dense(oracle_mod, p)
+    times = got["time"][:, 0]
+    # slices at 0, 0.02 and 0.04 from the continuous extension (the steps are
+    # not shortened); the buffer of three is full, so the wrap-up adds none
+    np.testing.assert_allclose(times, [0.0, 0.02, 0.04], atol=1e-14)
+    _compare_series(got, exp)
