@@ -349,6 +349,78 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? (NEXT ? 3 : 4) : 2)) k_
   dh_max_store<T>(mx, outsc);
 }
 
+// update_h without the next stage input, one mode ahead: the ten loads of
+// the next mode (six S_ij, h1, h2, dh1, dh2) are issued before the
+// projection arithmetic of the current one, so a warp keeps them in flight
+// through its arithmetic
+template <typename T>
+__global__ void __launch_bounds__(256, 3) k_update_h_pf(
+    const C2<T> *__restrict__ s, const T *__restrict__ y, T *__restrict__ out,
+    const RhsScalars *rs, Geom g, int skip_pos, double *outsc) {
+  const long long M = g.M;
+  const TensorConsts<T> tc(rs);
+  T mx = 0;
+  const unsigned mz_magic = g.mz_magic;
+  const int mz_shift = g.mz_shift, logny = g.logny;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  C2<T> v[6];
+  HVals<T> hv;
+  auto load = [&](long long q, C2<T>(&vv)[6], HVals<T> &h) {
+    if (q != 0) {  // the zero mode has no sources (its spectra are not read)
+      vv[0] = s[q];
+      vv[1] = s[M + q];
+      vv[2] = s[2 * M + q];
+      vv[3] = s[3 * M + q];
+      vv[4] = s[5 * M + q];
+      vv[5] = s[6 * M + q];
+    } else {
+#pragma unroll
+      for (int a = 0; a < 6; ++a) vv[a] = mk2c<T>(0, 0);
+    }
+    tensor_load<T>(g, q, y, h);
+  };
+  if (id < M) load(id, v, hv);
+  while (id < M) {
+    const long long nid = id + stride;
+    C2<T> vn[6];
+    HVals<T> hn;
+    if (nid < M) {
+      load(nid, vn, hn);
+    } else {
+#pragma unroll
+      for (int a = 0; a < 6; ++a) vn[a] = mk2c<T>(0, 0);
+      hn.h1 = hn.h2 = hn.d1 = hn.d2 = mk2c<T>(0, 0);
+    }
+    const unsigned uid = (unsigned)id;
+    const unsigned r = (__umulhi(uid, mz_magic) + uid) >> mz_shift;
+    Mode m;
+    m.k = (int)(uid - r * (unsigned)g.mz);
+    if (g.pow2) {
+      m.j = (int)(r & (unsigned)(g.ny - 1));
+      m.i = (int)(r >> logny);
+    } else {
+      m.j = (int)(r % (unsigned)g.ny);
+      m.i = (int)(r / (unsigned)g.ny);
+    }
+    C2<T> n0 = mk2c<T>(0, 0), n1 = mk2c<T>(0, 0);
+    T ksq = 0;
+    if (id != 0) {
+      const ModeK<T> q = mode_k<T>(g, m);
+      ksq = q.ksq;
+      tensor_sources<T>(m, q, v, n0, n1);
+    }
+    C2<T> o3, o4;
+    tensor_eom_core<T>(g, id, n0, n1, ksq, tc, hv, out, skip_pos, o3, o4);
+    mx = fmax(mx, fmax(fmax(fabs(o3.x), fabs(o3.y)), fmax(fabs(o4.x), fabs(o4.y))));
+#pragma unroll
+    for (int a = 0; a < 6; ++a) v[a] = vn[a];
+    hv = hn;
+    id = nid;
+  }
+  dh_max_store<T>(mx, outsc);
+}
+
 // The last forward x pass of the six S_ij spectra (arrays 0..3, 5, 6 of
 // spec; z and y passes done) and update_h, writing the tensor segments of
 // out: x passes then k_update_h, or the fused k_fft_x_tensor, as the
@@ -368,7 +440,9 @@ static int tensor_last_pass_t(Ctx *c, C2<T> *s, T *y, T *out, double *outsc,
   prof_begin(c, KK_UPDATE_H);
   if (next) {
     k_update_h<T, true><<<gm, 256, 0, c->stream>>>(s, y, out, c->rs, g, *next, outsc);
-  } else {
+  } else if constexpr (sizeof(T) == 4) {
+    k_update_h_pf<T><<<gm, 256, 0, c->stream>>>(s, y, out, c->rs, g, c->skip_pos, outsc);
+  } else {  // FP64: ALU-bound; the prefetching form would spill
     NextLin none{};
     none.skip_pos = c->skip_pos;
     k_update_h<T, false><<<gm, 256, 0, c->stream>>>(s, y, out, c->rs, g, none, outsc);

@@ -202,30 +202,59 @@ __device__ __forceinline__ void nl_apply_c(const NextLin &nl, T dt, long long e,
 // input at the same entries of y (nl, dt = the step size in T).  Returns the
 // largest |component| of the two dh' values (the FP32 noise scale of the
 // tensor sources, see k_dopri_final).
+// the tensor entries of mode id: h1, h2, dh1, dh2 (complex values at 2 id of
+// each segment; Nh1, Next are even)
+template <typename T>
+struct HVals {
+  C2<T> h1, h2, d1, d2;
+};
+template <typename T>
+__device__ __forceinline__ void tensor_load(const Geom &g, long long id, const T *y, HVals<T> &v) {
+  const long long N = g.N, Next = g.Next;
+  const long long Nh1 = 4 * N, Nh2 = Nh1 + Next, Ndh1 = Nh2 + Next, Ndh2 = Ndh1 + Next;
+  const C2<T> *yv = reinterpret_cast<const C2<T> *>(y);
+  v.h1 = yv[Nh1 / 2 + id];
+  v.h2 = yv[Nh2 / 2 + id];
+  v.d1 = yv[Ndh1 / 2 + id];
+  v.d2 = yv[Ndh2 / 2 + id];
+}
+
+// h' = dh (unless skip_pos) and dh' of mode id into out; returns dh1', dh2'
+template <typename T>
+__device__ __forceinline__ void tensor_eom_core(const Geom &g, long long id, C2<T> n0, C2<T> n1,
+                                                T ksq, const TensorConsts<T> &tc,
+                                                const HVals<T> &v, T *__restrict__ out,
+                                                int skip_pos, C2<T> &o3, C2<T> &o4) {
+  const long long N = g.N, Next = g.Next;
+  const long long Nh1 = 4 * N, Nh2 = Nh1 + Next, Ndh1 = Nh2 + Next, Ndh2 = Ndh1 + Next;
+  const T tm = -(tc.pm2 + ksq * tc.inv_a2);
+  C2<T> *ov = reinterpret_cast<C2<T> *>(out);
+  o3 = mk2c<T>(tm * v.h1.x - tc.h3 * v.d1.x + tc.two_inv_a2 * n0.x,
+               tm * v.h1.y - tc.h3 * v.d1.y + tc.two_inv_a2 * n0.y);
+  o4 = mk2c<T>(tm * v.h2.x - tc.h3 * v.d2.x + tc.two_inv_a2 * n1.x,
+               tm * v.h2.y - tc.h3 * v.d2.y + tc.two_inv_a2 * n1.y);
+  if (!skip_pos) {
+    ov[Nh1 / 2 + id] = v.d1;
+    ov[Nh2 / 2 + id] = v.d2;
+  }
+  ov[Ndh1 / 2 + id] = o3;
+  ov[Ndh2 / 2 + id] = o4;
+}
+
 template <typename T, bool NEXT>
 __device__ __forceinline__ T tensor_eom(const Geom &g, long long id, C2<T> n0, C2<T> n1, T ksq,
                                            const TensorConsts<T> &tc, T *y, T *__restrict__ out,
                                            const NextLin &nl, T dt) {
   const long long N = g.N, Next = g.Next;
   const long long Nh1 = 4 * N, Nh2 = Nh1 + Next, Ndh1 = Nh2 + Next, Ndh2 = Ndh1 + Next;
-  const T tm = -(tc.pm2 + ksq * tc.inv_a2);
   typedef C2<T> V;
   V *yv = reinterpret_cast<V *>(y);
-  V *ov = reinterpret_cast<V *>(out);
-  // the tensor segments hold complex values at 2 id (Nh1, Next are even)
   const long long e1 = Nh1 / 2 + id, e2 = Nh2 / 2 + id, e3 = Ndh1 / 2 + id, e4 = Ndh2 / 2 + id;
-  const V h1 = yv[e1], h2 = yv[e2];
-  const V d1 = yv[e3], d2 = yv[e4];
-  const V o3 = mk2c<T>(tm * h1.x - tc.h3 * d1.x + tc.two_inv_a2 * n0.x,
-                       tm * h1.y - tc.h3 * d1.y + tc.two_inv_a2 * n0.y);
-  const V o4 = mk2c<T>(tm * h2.x - tc.h3 * d2.x + tc.two_inv_a2 * n1.x,
-                       tm * h2.y - tc.h3 * d2.y + tc.two_inv_a2 * n1.y);
-  if (!nl.skip_pos) {
-    ov[e1] = d1;
-    ov[e2] = d2;
-  }
-  ov[e3] = o3;
-  ov[e4] = o4;
+  HVals<T> hv;
+  tensor_load<T>(g, id, y, hv);
+  const V d1 = hv.d1, d2 = hv.d2;
+  V o3, o4;
+  tensor_eom_core<T>(g, id, n0, n1, ksq, tc, hv, out, nl.skip_pos, o3, o4);
   if constexpr (NEXT) {
     nl_apply_c<T>(nl, dt, e1, d1, yv);
     nl_apply_c<T>(nl, dt, e2, d2, yv);
