@@ -142,7 +142,8 @@ class Clocks:
                 "samples": len(sm)}
 
 
-ENGINE_NAMES = {0: "stockham", 1: "two-step", 2: "two-step-half", 3: "pipelined", 4: "three-step"}
+ENGINE_NAMES = {0: "stockham", 1: "two-step", 2: "two-step-half", 3: "pipelined", 4: "three-step",
+                5: "two-step-half-occ"}
 
 
 def make_context(gpu, precision, device):

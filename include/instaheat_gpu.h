@@ -194,10 +194,12 @@ const char *ih_autotune_report(const ih_context *c);
  * engine IH_FFT_STOCKHAM, IH_FFT_TWOSTEP (register two-step,
  * 128-byte tiles), IH_FFT_TWOSTEP_HALF (64-byte tiles), IH_FFT_PIPELINED
  * (register two-step in persistent CTAs that copy the next tile in with
- * cp.async while transforming the current one) or IH_FFT_THREESTEP (three
- * register steps of at most 8 values; passes 0 and 1 only). */
+ * cp.async while transforming the current one), IH_FFT_THREESTEP (three
+ * register steps of at most 8 values; passes 0 and 1 only) or
+ * IH_FFT_TWOSTEP_HALF_OCC (IH_FFT_TWOSTEP_HALF compiled for 7 resident CTAs
+ * per SM; passes 0 and 1, FP32; FP64 runs IH_FFT_TWOSTEP_HALF). */
 enum { IH_FFT_STOCKHAM = 0, IH_FFT_TWOSTEP = 1, IH_FFT_TWOSTEP_HALF = 2, IH_FFT_PIPELINED = 3,
-       IH_FFT_THREESTEP = 4 };
+       IH_FFT_THREESTEP = 4, IH_FFT_TWOSTEP_HALF_OCC = 5 };
 int ih_fft_set_engine(ih_context *c, int pass, int engine);
 int ih_fft_get_engine(const ih_context *c, int pass);
 /* How an RHS without the filter and output flags forms the derivatives of

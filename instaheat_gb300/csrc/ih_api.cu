@@ -507,7 +507,7 @@ int ih_fft_set_engine(ih_context *h, int pass, int engine) {
     return IH_OK;
   }
   if (pass < 0 || pass > 6 || engine < 0 || engine >= FV_COUNT) return IH_ERR_ARG;
-  if (pass == 2 && engine == FV_THREESTEP) return IH_ERR_ARG;
+  if (pass == 2 && (engine == FV_THREESTEP || engine == FV_TWOSTEP_HALF_OCC)) return IH_ERR_ARG;
   if ((pass == 3 || pass == 4) && engine != FV_TWOSTEP && engine != FV_TWOSTEP_HALF)
     return IH_ERR_ARG;
   if (pass >= 5 && engine > 1) return IH_ERR_ARG;

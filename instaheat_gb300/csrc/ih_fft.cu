@@ -337,6 +337,60 @@ __global__ void __launch_bounds__(pass_threads<L, B>()) k_fft_xy_2s(C2<T> *data,
   }
 }
 
+// the body of k_fft_xy_2s for the variant below
+template <typename T, int L, int B>
+__device__ __forceinline__ void xy_2s_body(C2<T> *data, long long astride, long long sj,
+                                           long long so, int mz, int sign, const C2<T> *twg) {
+  constexpr int R1 = Fac<L>::R1, R2 = Fac<L>::R2;
+  constexpr int LB = clog2(B), P = B;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<T> *tw = reinterpret_cast<C2<T> *>(smraw);
+  C2<T> *x1 = tw + L;  // [n1*R2 + k2][P]
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int z0 = blockIdx.x * B;
+  const int bv = min(B, mz - z0);
+  C2<T> *base = data + blockIdx.z * astride + (long long)blockIdx.y * so + z0;
+  load_table(tw, twg, L, tid, nt);
+  __syncthreads();
+  if (tid < R1 * B) {
+    const int b = tid & (B - 1), n1 = tid >> LB;
+    C2<T> v[R2];
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2)
+      v[n2] = (b < bv) ? base[(long long)(n1 + R1 * n2) * sj + b] : mk2<T>(0, 0);
+    reg_dft<T, R2>(v, tw, L / R2, sign);
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2)
+      x1[xrow<L>(n1 * R2 + k2) * P + b] = (k2 == 0) ? v[k2] : cmul(v[k2], twid(tw, (n1 * k2) & (L - 1), sign));
+  }
+  __syncthreads();
+  if (tid < R2 * B) {
+    const int b = tid & (B - 1), k2 = tid >> LB;
+    C2<T> u[R1];
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) u[n1] = x1[xrow<L>(n1 * R2 + k2) * P + b];
+    reg_dft<T, R1>(u, tw, L / R1, sign);
+    if (b < bv) {
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) base[(long long)(k2 + R2 * k1) * sj + b] = u[k1];
+    }
+  }
+}
+
+// The same engine compiled for more resident CTAs (FV_TWOSTEP_HALF_OCC, FP32):
+// 1280 threads per SM (10 CTAs of 128 at L = 256: at most 51 registers
+// instead of the 80 the plain build takes, fewer loads in flight per warp,
+// more warps); the autotuner keeps it only where it is faster.
+template <int L, int B> __host__ __device__ constexpr int occ_min_blocks() {
+  return 1280 / pass_threads<L, B>() > 1 ? 1280 / pass_threads<L, B>() : 1;
+}
+template <typename T, int L, int B>
+__global__ void __launch_bounds__(pass_threads<L, B>(), (occ_min_blocks<L, B>())) k_fft_xy_2s_occ(
+    C2<T> *data, long long astride, long long sj, long long so, int mz, int sign,
+    const C2<T> *twg) {
+  xy_2s_body<T, L, B>(data, astride, sj, so, mz, sign, twg);
+}
+
 // ---------------------------------------------------------------------------
 // Three-step engine: L = R1 R2 with R2 <= 8 held per thread, and the R1-point
 // DFTs of step 2 themselves split as R1 = Ra Rb, so no thread holds more than
@@ -1601,6 +1655,15 @@ struct XYLaunch {
     return IH_OK;
   }
   template <int L, int B>
+  int run_2s_occ(dim3 grid, long long sj, long long so, const C2<T> *tw) {
+    const size_t sm = sizeof(C2<T>) * ((size_t)L + (size_t)L * B);
+    cudaFuncSetAttribute(k_fft_xy_2s_occ<T, L, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm);
+    k_fft_xy_2s_occ<T, L, B><<<grid, pass_threads<L, B>(), sm, c->stream>>>(data, stride, sj, so,
+                                                                             mzv(), sign, tw);
+    return IH_OK;
+  }
+  template <int L, int B>
   int run_pipe(long long sj, long long so, int outer, const C2<T> *tw) {
     const Geom &g = c->g;
     const size_t sm = sizeof(C2<T>) * ((size_t)L + 2 * (size_t)L * B);
@@ -1649,10 +1712,17 @@ struct XYLaunch {
           return run_2s<L, B>(dim3((mz + B - 1) / B, outer, count), sj, so, tw);
         }
       }
-      const int bw = var == FV_TWOSTEP_HALF ? B / 2 : B;
+      const int bw = (var == FV_TWOSTEP_HALF || var == FV_TWOSTEP_HALF_OCC) ? B / 2 : B;
       dim3 grid((mz + bw - 1) / bw, outer, count);
       if (var == FV_TWOSTEP) return run_2s<L, B>(grid, sj, so, tw);
       if (var == FV_TWOSTEP_HALF) return run_2s<L, B / 2>(grid, sj, so, tw);
+      if (var == FV_TWOSTEP_HALF_OCC) {
+        if constexpr (sizeof(T) == 4) {
+          return run_2s_occ<L, B / 2>(grid, sj, so, tw);
+        } else {  // FP64: the plain half-line engine
+          return run_2s<L, B / 2>(grid, sj, so, tw);
+        }
+      }
       return run_st<B>(L, grid, sj, so, tw);
     }
   }
@@ -2094,8 +2164,8 @@ int fft_tables(Ctx *c) {
 // with CUDA events on the context stream over zeroed scratch spectra; the
 // fastest is kept.  Transform timing does not depend on the data.
 static const char *variant_name(int v) {
-  static const char *names[FV_COUNT] = {"stockham", "two-step", "two-step-half", "pipelined",
-                                        "three-step"};
+  static const char *names[FV_COUNT] = {"stockham",  "two-step",   "two-step-half",
+                                        "pipelined", "three-step", "two-step-half-occ"};
   return (v >= 0 && v < FV_COUNT) ? names[v] : "unknown";
 }
 
@@ -2130,7 +2200,8 @@ static int autotune_t(Ctx *c) {
     int best = -1;
     float tbest = 0.f;
     for (int v = 0; v < FV_COUNT && st == IH_OK; ++v) {
-      if (pass == 2 && v == FV_THREESTEP) continue;  // the fused x pass has no three-step form
+      if (pass == 2 && (v == FV_THREESTEP || v == FV_TWOSTEP_HALF_OCC))
+        continue;  // the fused x pass has neither form
       if (pass > 2 && v != FV_TWOSTEP && v != FV_TWOSTEP_HALF) continue;
       if (pass < 2) {
         c->xy_var[pass] = v;

@@ -129,6 +129,7 @@ enum FftVariant {
   FV_TWOSTEP_HALF = 2,  // register two-step, tile of half a line
   FV_PIPELINED = 3,     // register two-step, persistent CTAs, cp.async double buffering
   FV_THREESTEP = 4,     // three register steps of <= 8 values (x/y passes only)
+  FV_TWOSTEP_HALF_OCC = 5,  // FV_TWOSTEP_HALF compiled for 7 CTAs per SM (x/y passes, FP32)
   FV_COUNT
 };
 

@@ -20,6 +20,7 @@ from . import build as _build
 PREC_F64 = 0
 PREC_MIXED = 1
 FFT_STOCKHAM, FFT_TWOSTEP, FFT_TWOSTEP_HALF, FFT_PIPELINED, FFT_THREESTEP = 0, 1, 2, 3, 4
+FFT_TWOSTEP_HALF_OCC = 5
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed",
           4: "call out of order", 5: "step size underflow", 6: "non-finite value"}

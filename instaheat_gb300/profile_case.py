@@ -115,7 +115,7 @@ def main(argv=None):
     ctx = gpu.Context(n=(args.n,) * 3, precision=prec)
     if args.engine is not None:  # pin the x/y (and, where it exists, fused x) FFT engine
         for p in range(3):
-            if not (p == 2 and args.engine == gpu.FFT_THREESTEP):
+            if not (p == 2 and args.engine in (gpu.FFT_THREESTEP, gpu.FFT_TWOSTEP_HALF_OCC)):
                 ctx.set_engine(p, args.engine)
     elif args.autotune:
         print(ctx.autotune(wisdom=True), flush=True)

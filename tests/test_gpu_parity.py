@@ -223,13 +223,16 @@ def test_mean_dev_matches_numpy(gpu_mod):
     assert abs(out.item() - ref) <= 1e-13 * abs(ref)
 
 
-ENGINES = [0, 1, 2, 3, 4]  # Stockham, two-step, two-step (64-byte tiles), pipelined, three-step
+# Stockham, two-step, two-step (64-byte tiles), pipelined, three-step,
+# two-step (64-byte tiles) compiled for 7 CTAs per SM
+ENGINES = [0, 1, 2, 3, 4, 5]
 
 
 def pin_engine(ctx, engine):
-    """Pin every pass to the engine (the fused x pass has no three-step form)."""
+    """Pin every pass to the engine (the fused x pass has no three-step
+    form and no 7-CTA form)."""
     for p in range(3):
-        if not (p == 2 and engine == 4):
+        if not (p == 2 and engine in (4, 5)):
             ctx.set_engine(p, engine)
 
 
