@@ -47,7 +47,8 @@ def test_render_template_substitution():
     assert r == "#define MASS (4.0)\n#define ENABLE_GW\n#define NOT_OUTPUT_PHI\n"
 
 
-@pytest.mark.parametrize("name", ["parameters_dopri853.sh", "parameters_rk4.sh"])
+@pytest.mark.parametrize("name", ["parameters_dopri853.sh", "parameters_rk4.sh",
+                                  "parameters_landing.sh", "parameters_dense.sh"])
 def test_host_builds_warning_free(tmp_path, name):
     exe = dropin.build_host(PARAMS / name, tmp_path / "host")
     assert exe.exists()
