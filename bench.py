@@ -32,6 +32,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -93,16 +94,19 @@ class Dist:
 
 
 class Clocks:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling during the timed region; the raw
+    samples go to $IH_CLOCKS_DIR/clocks_rank<i>.csv (default: the system's
+    temporary directory)."""
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_rank{gpu_index}.csv"
+        self.path = (Path(os.environ.get("IH_CLOCKS_DIR", tempfile.gettempdir())) /
+                     f"clocks_rank{gpu_index}.csv")
 
     def start(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
+            self.path.parent.mkdir(parents=True, exist_ok=True)
             self.f = open(self.path, "w")
             q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
