@@ -1000,7 +1000,7 @@ static int lincomb_vel(Ctx *c, int s) {
   VelLin a;
   const Vec *stage[12];
   for (int l = 0; l < 12; ++l) stage[l] = &c->k[l + 1];
-  IH_TRY(vel_terms(s, stage, a));
+  vel_terms(s, stage, a);  // every stage vector is present
   const int n = a.n;
   a.dt = c->dt_dev;
   const Geom &g = c->g;
@@ -1424,7 +1424,10 @@ int dopri_dense(Ctx *c, double t_out, int want_output) {
       for (int l = 0; l < 12; ++l) vst[l] = st[l];
       for (int s = 5; s < 12; ++s) {
         VelLin a;
-        IH_TRY(vel_terms(s, vst, a));
+        if (vel_terms(s, vst, a) != IH_OK) {
+          c->err = "dense output: a stage input needs stage 2, which the step no longer holds";
+          return IH_ERR_STATE;
+        }
         const long long nq = (2 * g.N + 2 * g.Next) / 4;
         prof_begin(c, KK_LINCOMB);
         k_restore_pos<<<stream_grid(nq), 256, 0, c->stream>>>(
@@ -1438,7 +1441,10 @@ int dopri_dense(Ctx *c, double t_out, int want_output) {
       memset(&a, 0, sizeof a);
       for (int j = 0; j < 13 + r; ++j) {
         if (DAD[r][j] == 0.0) continue;
-        if (!st[j] || a.n == kMaxTerms) return IH_ERR_STATE;  // fixed by the tableau
+        if (!st[j] || a.n == kMaxTerms) {  // fixed by the tableau: never taken
+          c->err = "dense output: unexpected term list of an extra stage";
+          return IH_ERR_STATE;
+        }
         a.in[a.n] = st[j]->fl;
         a.insc[a.n] = st[j]->sc;
         a.coef[a.n] = DAD[r][j];
@@ -1462,7 +1468,10 @@ int dopri_dense(Ctx *c, double t_out, int want_output) {
     if (j == 0) w += th * s1 * s1;
     if (j == 12) w -= th * th * s1;
     if (w == 0.0) continue;
-    if (a.n == kMaxTerms) return IH_ERR_STATE;  // 12 weighted stages at most
+    if (a.n == kMaxTerms) {  // 12 weighted stages at most: never taken
+      c->err = "dense output: unexpected term list of the interpolant";
+      return IH_ERR_STATE;
+    }
     a.in[a.n] = st[j]->fl;
     a.insc[a.n] = st[j]->sc;
     a.coef[a.n] = w;
