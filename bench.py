@@ -14,7 +14,8 @@ psi from the constraints), GW on, filter on, DOPRI853 rtol = atol = 1e-8.
             uploads the state from pinned host memory, steps, and downloads
             the new state.
   f64    -- the plain FP64 form on the same workload (the ratio the metric
-            names).
+            names), with its step against both of its bounds: algorithmic
+            bytes vs the HBM copy peak, flops vs the FP64 pipe.
   roofline -- the kernel with the largest share of device time in the timed
             region: algorithmic bytes per launch / mean launch time (CUDA
             events around each launch), against the measured HBM copy peak.
@@ -214,16 +215,38 @@ def bench_form(gpu, precision, device, seed, steps, warmup, profile=False, clock
     return ctx, res
 
 
-def step_roofline(ms_per_step, peak, peak_src):
+def step_roofline(ms_per_step, peak, peak_src, elem=4):
     n = N_GRID
     N = n ** 3
     Next = 2 * n * n * (n // 2 + 1)
     Ntot = 4 * N + 4 * Next + 1
-    b_step = (12 * 15 * (N + Next) + 72 * Ntot) * 4
+    b_step = (12 * 15 * (N + Next) + 72 * Ntot) * elem
     achieved = b_step / (ms_per_step / 1e3) / 1e9
     return {"bytes_per_step": b_step, "achieved": achieved, "peak": peak, "peak_source": peak_src,
             "unit": "GB/s", "frac": achieved / peak,
             "floor_ms_per_step": b_step / (peak * 1e9) * 1e3}
+
+
+# FP64 FMA rate of a GB300 (nominal; the pipe the FP64 form's FFTs run on)
+FP64_NOMINAL_TFLOPS = 1.25
+
+
+def f64_roofline(ms_per_step, peak, peak_src):
+    """Both bounds of the plain FP64 form: its algorithmic bytes (the
+    per-step formula at 8 bytes per value) against the HBM copy peak, and its
+    flops -- 12 RHS x 11 transforms x 2.5 N log2 N plus about 160 Ntot in the
+    stage combinations -- against the FP64 pipe."""
+    n = N_GRID
+    N = n ** 3
+    Next = 2 * n * n * (n // 2 + 1)
+    Ntot = 4 * N + 4 * Next + 1
+    flops = 12 * 11 * 2.5 * N * np.log2(N) + 160 * Ntot
+    tflops = flops / (ms_per_step / 1e3) / 1e12
+    hbm = step_roofline(ms_per_step, peak, peak_src, elem=8)
+    alu = {"flops_per_step": flops, "achieved": tflops, "peak": FP64_NOMINAL_TFLOPS,
+           "peak_source": "nominal", "unit": "TFLOP/s", "frac": tflops / FP64_NOMINAL_TFLOPS,
+           "floor_ms_per_step": flops / (FP64_NOMINAL_TFLOPS * 1e12) * 1e3}
+    return {"bound": "fp64" if alu["frac"] >= hbm["frac"] else "hbm", "hbm": hbm, "fp64": alu}
 
 
 def bench_e2e(gpu, ctx, steps):
@@ -390,8 +413,10 @@ def main():
         }
         if f64:
             f64v = f64["mt"] / (f64["ms"] / 1e3)
-            line["f64"] = {"value": f64v, "unit": UNIT, "ms_per_step": f64["ms"] / max(1, min(steps, 3)),
-                           "dt_next": f64["dt_next"]}
+            ms64 = f64["ms"] / max(1, min(steps, 3))
+            line["f64"] = {"value": f64v, "unit": UNIT, "ms_per_step": ms64,
+                           "dt_next": f64["dt_next"],
+                           "roofline": f64_roofline(ms64, peak, peak_src)}
             line["speedup_vs_f64"] = value / f64v
         if acc:
             line["accuracy_vs_f64"] = acc

@@ -56,3 +56,14 @@ def test_committed_bench_record_has_the_contract_keys():
         assert k in c, k
     acc = d["accuracy_vs_f64"]
     assert acc["within_1pct"] is True and acc["gw_max_rel_diff"] < 0.01
+
+
+def test_f64_form_bounds():
+    """The FP64 form against both of its bounds at 256^3: 126.1 GB per step
+    against HBM, 1.54e11 flops against the FP64 pipe -- the pipe binds."""
+    b = _bench()
+    r = b.f64_roofline(274.0, 6778.3, "measured")
+    assert r["hbm"]["bytes_per_step"] == 2 * 63_059_263_776
+    assert abs(r["fp64"]["flops_per_step"] - 1.5443e11) < 1e8
+    assert abs(r["fp64"]["floor_ms_per_step"] - 123.5) < 0.5
+    assert r["bound"] == "fp64" and r["fp64"]["frac"] > r["hbm"]["frac"]
