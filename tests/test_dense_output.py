@@ -119,3 +119,47 @@ def test_gpu_dense_tableau_equals_oracle(gpu_mod, oracle_mod):
     """The library's dense-output coefficients (no GPU needed to read them)."""
     for x, y in zip(gpu_mod.dense_tableau(), oracle_mod.dense_tableau()):
         assert np.array_equal(x, y)
+
+
+def test_oracle_dense_matches_a_numpy_dop853_step(oracle_mod):
+    """The oracle's dense output against an independent numpy DOP853 step on
+    the numpy restatement of the RHS (oracle/rhs_numpy.py, pocketfft): the
+    same stages, the post-step RHS filtering field_new, stages 14-16 and the
+    nested interpolant, to 1e-11 of each state segment's largest magnitude."""
+    from oracle.rhs_numpy import NumpyRHS
+    n, L = (16, 16, 8), (20.0, 18.0, 14.0)
+    o = oracle_mod.Oracle(n=n, L=L)
+    nr = NumpyRHS(n, L)
+    f = o.ic(seed=4, amp=1e-3)
+    f[4 * o.N:-1] = 1e-6 * np.random.default_rng(4).standard_normal(4 * o.Next)
+    cfg = oracle_mod.default_cfg(1e-9, 1e-9, 1e-2)
+    st, df = o.dopri_init(f, cfg, 0.0, 2e-2)   # filters f in place, df = f(f)
+    y0, k1 = f.copy(), df.copy()
+    thetas = [0.25, 0.6, 1.0]
+    rc, dense = o.dopri_step_dense(f, df, cfg, st, 2e-2, thetas)
+    assert rc == 0 and st.dt_did == 2e-2
+    h = st.dt_did
+    c, a, b, bhh, er = oracle_mod.tableau()
+    ad, d = oracle_mod.dense_tableau()
+    k = [k1]
+    for s_ in range(1, 12):
+        k.append(nr.rhs(y0 + h * sum(a[s_, j] * k[j] for j in range(s_)))[0])
+    ynew = y0 + h * sum(b[j] * k[j] for j in range(12))
+    k13, ynew_f, _ = nr.rhs(ynew, filter=1)
+    k.append(k13)
+    for r in range(3):
+        k.append(nr.rhs(y0 + h * sum(ad[r, j] * k[j] for j in range(13 + r)))[0])
+    K = np.array(k)
+    for q, th in enumerate(thetas):
+        s = 1.0 - th
+        r1, r2 = y0, ynew_f - y0
+        r3 = h * k1 - r2
+        r4 = r2 - h * k13 - r3
+        r5, r6, r7, r8 = (h * (d[i] @ K) for i in range(4))
+        ref = r1 + th * (r2 + s * (r3 + th * (r4 + s * (r5 + th * (r6 + s * (r7 + th * r8))))))
+        N, Next = o.N, o.Next
+        edges = [0, N, 2 * N, 3 * N, 4 * N] + [4 * N + i * Next for i in range(1, 5)]
+        for lo, hi in zip(edges[:-1], edges[1:]):  # each segment on its own scale
+            seg = slice(lo, hi)
+            assert np.abs(dense[q][seg] - ref[seg]).max() <= 1e-11 * np.abs(ref[seg]).max(), (th, lo)
+        assert abs(dense[q][-1] / ref[-1] - 1.0) < 1e-13
