@@ -122,10 +122,12 @@ def test_gpu_dense_tableau_equals_oracle(gpu_mod, oracle_mod):
 
 
 def test_oracle_dense_matches_a_numpy_dop853_step(oracle_mod):
-    """The oracle's dense output against an independent numpy DOP853 step on
-    the numpy restatement of the RHS (oracle/rhs_numpy.py, pocketfft): the
-    same stages, the post-step RHS filtering field_new, stages 14-16 and the
-    nested interpolant, to 1e-11 of each state segment's largest magnitude."""
+    """The oracle's DOPRI853 step and dense output against an independent
+    numpy DOP853 step on the numpy restatement of the RHS
+    (oracle/rhs_numpy.py, pocketfft): the error norm of the accepted try to
+    1e-6 relative, and the post-step RHS filtering field_new, stages 14-16 and
+    the nested interpolant to 1e-11 of each state segment's largest
+    magnitude."""
     from oracle.rhs_numpy import NumpyRHS
     n, L = (16, 16, 8), (20.0, 18.0, 14.0)
     o = oracle_mod.Oracle(n=n, L=L)
@@ -133,18 +135,28 @@ def test_oracle_dense_matches_a_numpy_dop853_step(oracle_mod):
     f = o.ic(seed=4, amp=1e-3)
     f[4 * o.N:-1] = 1e-6 * np.random.default_rng(4).standard_normal(4 * o.Next)
     cfg = oracle_mod.default_cfg(1e-9, 1e-9, 1e-2)
-    st, df = o.dopri_init(f, cfg, 0.0, 2e-2)   # filters f in place, df = f(f)
+    st, df = o.dopri_init(f, cfg, 0.0, 0.1)   # filters f in place, df = f(f)
     y0, k1 = f.copy(), df.copy()
     thetas = [0.25, 0.6, 1.0]
-    rc, dense = o.dopri_step_dense(f, df, cfg, st, 2e-2, thetas)
-    assert rc == 0 and st.dt_did == 2e-2
-    h = st.dt_did
+    # a long step, so that the error estimate stands well above FP64 rounding
+    rc, dense = o.dopri_step_dense(f, df, cfg, st, 0.1, thetas)
+    assert rc == 0
+    h = st.dt_did  # the accepted try's size (the last try's stages)
     c, a, b, bhh, er = oracle_mod.tableau()
     ad, d = oracle_mod.dense_tableau()
     k = [k1]
     for s_ in range(1, 12):
         k.append(nr.rhs(y0 + h * sum(a[s_, j] * k[j] for j in range(s_)))[0])
     ynew = y0 + h * sum(b[j] * k[j] for j in range(12))
+    # the error norm of the accepted try (dopri853.c:438-486), a cancellation
+    # of the stages, which the C and numpy code round differently
+    kb = sum(b[j] * k[j] for j in range(12))
+    yerr = kb - bhh[0] * k[0] - bhh[1] * k[8] - bhh[2] * k[11]
+    yerr2 = sum(er[j] * k[j] for j in range(12))
+    sk = cfg.atol + cfg.rtol * np.maximum(np.abs(y0), np.abs(ynew))
+    e2, e3 = np.sum((yerr / sk) ** 2), np.sum((yerr2 / sk) ** 2)
+    err = h * e3 * np.sqrt(1.0 / (o.Ntot * (e3 + 0.01 * e2)))
+    assert st.last_err > 1e-4 and abs(err / st.last_err - 1.0) < 1e-6, (err, st.last_err)
     k13, ynew_f, _ = nr.rhs(ynew, filter=1)
     k.append(k13)
     for r in range(3):
