@@ -166,3 +166,28 @@ def test_rk4_step_reduces_to_background(oracle_mod):
         t += dt
     assert abs(f[0] - g["phi"][1]) < 1e-8
     assert abs(f[-1] - g["a"][1]) < 1e-8
+
+
+def test_c_oracle_rk4_step_matches_numpy(oracle_mod):
+    """rk4.c:108-161 (filter on the first stage only): the oracle's RK4 step
+    against the same step on the numpy restatement of the RHS, to 1e-12 of
+    each state segment's largest magnitude."""
+    from oracle.rhs_numpy import NumpyRHS
+    n, L = (16, 16, 8), (20.0, 18.0, 14.0)
+    o = oracle_mod.Oracle(n=n, L=L)
+    nr = NumpyRHS(n, L)
+    f = o.ic(seed=6, amp=1e-3)
+    f[4 * o.N:-1] = 1e-6 * np.random.default_rng(6).standard_normal(4 * o.Next)
+    dt = 0.01
+    k1, y, _ = nr.rhs(f, filter=1)
+    k2 = nr.rhs(y + dt * k1 / 2.0)[0]
+    k3 = nr.rhs(y + dt * k2 / 2.0)[0]
+    k4 = nr.rhs(y + dt * k3)[0]
+    ref = y + dt * (k1 + 2.0 * k2 + 2.0 * k3 + k4) / 6.0
+    got = f.copy()
+    o.rk4_step(got, 0.0, dt)
+    N, Next = o.N, o.Next
+    edges = [0, N, 2 * N, 3 * N, 4 * N] + [4 * N + i * Next for i in range(1, 5)]
+    for lo, hi in zip(edges[:-1], edges[1:]):
+        assert np.abs(got[lo:hi] - ref[lo:hi]).max() <= 1e-12 * np.abs(ref[lo:hi]).max(), lo
+    assert abs(got[-1] / ref[-1] - 1.0) < 1e-14
