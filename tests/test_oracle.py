@@ -191,3 +191,31 @@ def test_c_oracle_rk4_step_matches_numpy(oracle_mod):
     for lo, hi in zip(edges[:-1], edges[1:]):
         assert np.abs(got[lo:hi] - ref[lo:hi]).max() <= 1e-12 * np.abs(ref[lo:hi]).max(), lo
     assert abs(got[-1] / ref[-1] - 1.0) < 1e-14
+
+
+def test_c_oracle_psi_solve_matches_numpy(oracle_mod):
+    """mk_initial_psi (setup.c:825-903) restated on the numpy RHS: with psi
+    and dpsi zeroed, psi_k = (-<dphi> ddphi_k + <ddphi'> dphi_k) /
+    (-<dphi>^2 + 2 k^2 / a^2) (k = 0 mode zero), dpsi = <dphi>/2 dphi - H psi;
+    against the oracle to 1e-11 of each segment's largest magnitude."""
+    from oracle.rhs_numpy import NumpyRHS
+    n, L = (16, 16, 8), (20.0, 18.0, 14.0)
+    o = oracle_mod.Oracle(n=n, L=L)
+    nr = NumpyRHS(n, L)
+    f = o.ic(seed=7, amp=1e-3, psi=False)
+    N = o.N
+    g = f.copy()
+    g[2 * N:4 * N] = 0.0
+    res, _, dg = nr.rhs(g)
+    a2 = g[-1] ** 2
+    H = np.sqrt(dg["rho_mean"] / 3.0)
+    phim, dphim, ddphim = g[:N].mean(), g[N:2 * N].mean(), res[N:2 * N].mean()
+    D = nr.fft(g[N:2 * N] - dphim)
+    F = nr.fft(g[:N] - phim)
+    P = (-dphim * D + ddphim * F) / (-dphim ** 2 + 2.0 * nr.g["sq"] / a2)
+    P.flat[0] = 0.0
+    psi = np.fft.irfftn(P, s=n, axes=(0, 1, 2)).ravel()
+    dpsi = 0.5 * dphim * (g[:N] - phim) - H * psi
+    o.initial_psi(f)
+    assert np.abs(f[2 * N:3 * N] - psi).max() <= 1e-11 * np.abs(psi).max()
+    assert np.abs(f[3 * N:4 * N] - dpsi).max() <= 1e-11 * np.abs(dpsi).max()
