@@ -69,6 +69,16 @@ def test_c_oracle_matches_numpy_oracle(oracle_mod):
                 assert np.abs(got - dg[k]).max() <= 1e-12 * np.abs(dg[k]).max()
             # constraint residuals are cancellation-dominated: compare at 1e-6
             np.testing.assert_allclose(d.cstr, dg["cstr"], rtol=1e-6)
+            # summaries (toolbox.c:676-690): mean, variance (N - 1), min, max of
+            # phi, dphi, psi, dpsi of the (filtered) input state, rho and p
+            N = o.N
+            arrs = [f2[i * N:(i + 1) * N] for i in range(4)] + [dg["rho"], dg["p"]]
+            ref = np.array([[x.mean(), x.var(ddof=1), x.min(), x.max()] for x in arrs])
+            # means of zero-mean fields are rounding: a floor of 1e-12 of the
+            # field's magnitude per row
+            for row, x in zip(range(6), arrs):
+                np.testing.assert_allclose(d.smry[row], ref[row], rtol=1e-10,
+                                           atol=1e-12 * np.abs(x).max(), err_msg=str(row))
 
 
 def test_binning_rule(oracle_mod):
