@@ -1,10 +1,12 @@
 """CPU tests of the C-ABI boundary: the library builds, loads and exports every
-function include/*.h declares; host-only entry points behave (no GPU calls)."""
+function include/*.h declares; host-only entry points behave (no GPU calls);
+without a GPU the product path fails loudly."""
 import re
 import subprocess
 from pathlib import Path
 
 import numpy as np
+import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
 
@@ -52,3 +54,13 @@ def test_invalid_grid_is_rejected_before_any_device_call(gpu_mod):
     for n in bad:
         p = gpu_mod.Params(n[0], n[1], n[2], 20.0, 20.0, 20.0, 1.0, 1, 1, 8, 0, 0)
         assert L.ih_create(C.byref(p), C.byref(h)) == 1  # IH_ERR_ARG
+
+
+def test_no_gpu_fails_loudly(gpu_mod):
+    """Without a usable GPU the product path raises (no CPU fallback): context
+    creation reports the CUDA error instead of computing anything."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(gpu_mod.IHError, match="CUDA"):
+        gpu_mod.Context(n=(16, 16, 16))
