@@ -83,3 +83,24 @@ def test_dropin_compiles_against_reference_generated_headers(tmp_path):
                         "-I", str(PARAMS / "stubs"), "-I", str(dropin.ROOT / "include"),
                         str(dropin.HERE / "ih_dropin.c")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_host_without_gpu_exits_with_the_error(tmp_path):
+    """Without a GPU the drop-in does what the reference does on a failure:
+    a message on stderr and exit(EXIT_FAILURE) -- no CPU fallback."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import numpy as np
+    exe = dropin.build_host(PARAMS / "parameters_dopri853.sh", tmp_path / "host")
+    p = dropin.read_parameters(PARAMS / "parameters_dopri853.sh")
+    n = int(p["GRIDPOINTS_X"])
+    N, Next = n ** 3, 2 * n * n * (n // 2 + 1)
+    f = np.zeros(4 * N + 4 * Next + 1)
+    f[:N] = 1.0
+    f[-1] = 1.0
+    f.tofile(tmp_path / "init.bin")
+    r = subprocess.run([str(exe), str(tmp_path / "init.bin"), str(tmp_path / "out.ihc")],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0
+    assert "CUDA" in r.stderr or "CUDA" in r.stdout, (r.stdout, r.stderr)
