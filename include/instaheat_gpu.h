@@ -152,13 +152,18 @@ int ih_mean_dev(ih_context *c, const double *f_dev, size_t n, double *out_dev);
  * code without an ih_context).  No counterpart in the reference.
  * Scratch is a fixed 32 KiB array inside the library (held on every GPU that
  * loads it until the process exits); it is shared by all calls, so calls that
- * overlap on the GPU race and must be serialised by the caller.  The device
- * address of that array is looked up once per device by the first call made
- * on it, so make that first call before any stream capture.  n is limited to
- * ih_mean_dev_noalloc_max_n() = 2^28 doubles; larger n returns
- * IH_ERR_TOO_LARGE without launching anything.  Runs on `stream` (a
- * cudaStream_t; NULL = the legacy default stream) and returns without
- * waiting; *out_dev is device memory. */
+ * overlap on the GPU race and must be serialised by the caller.  The call
+ * runs on the calling thread's current CUDA device and uses that device's
+ * copy of the array: f_dev, out_dev and stream must all belong to it (unlike
+ * ih_mean_dev, which is tied to its context's device).  Each call looks the
+ * array's device address up in the current context; the first call in a
+ * context may load the library's kernels there, so make it before any
+ * stream capture.  n is limited to ih_mean_dev_noalloc_max_n() = 2^28
+ * doubles; larger n returns IH_ERR_TOO_LARGE without launching anything.
+ * Runs on `stream` (a cudaStream_t; NULL = the legacy default stream) and
+ * returns without waiting; *out_dev is device memory.  On IH_ERR_CUDA the
+ * CUDA error is left pending for the caller's cudaGetLastError (a pending
+ * error from the caller's earlier work also yields IH_ERR_CUDA). */
 int ih_mean_dev_noalloc(const double *f_dev, size_t n, double *out_dev, void *stream);
 size_t ih_mean_dev_noalloc_max_n(void);
 
@@ -418,6 +423,13 @@ unsigned long long ih_kernel_launches(const ih_context *c);
 /* ---- pinned host memory for end-to-end transfers ---- */
 int ih_host_alloc(size_t bytes, void **out);
 int ih_host_free(void *p);
+
+/* ---- measurement (no reference counterpart) ----
+ * FP64 FMA throughput of GPU `device` in TFLOP/s: independent DFMA chains in
+ * 8 CTAs of 256 threads per SM, `iters` links per chain, best of `reps`
+ * CUDA-event-timed launches after one warm-up.  The ALU roofline of the
+ * plain FP64 form. */
+int ih_fp64_fma_peak(int device, int iters, int reps, double *tflops);
 
 #ifdef __cplusplus
 }

@@ -23,12 +23,18 @@
 // IH_ERR_TOO_LARGE before anything is launched.
 //
 // Host code must not pass g_mean_scratch itself to a kernel: in host code the
-// name denotes a host-side stand-in, not the device address.  The device
-// address is fetched once per device with cudaGetSymbolAddress, with that
-// device current, on the first call made while it is the current device.
-// That first call should therefore come before any stream capture.
+// name denotes a host-side stand-in, not the device address.  Every call looks
+// the device address up with cudaGetSymbolAddress in the context current on
+// the calling thread, so a call after cudaDeviceReset (which reloads the
+// module at a possibly different address) or under another context of the
+// same device gets that context's copy.  The first call in a context may load
+// the module there, so make it before any stream capture.
+//
+// Errors: a failed lookup or launch returns IH_ERR_CUDA and leaves the CUDA
+// error pending (cudaPeekAtLastError, not cudaGetLastError), so the caller
+// reads its text with cudaGetLastError; an error already pending from the
+// caller's own earlier work is reported the same way and is not cleared.
 #include <cuda_runtime.h>
-#include <mutex>
 #include "../../include/instaheat_gpu.h"
 
 namespace {
@@ -36,12 +42,8 @@ namespace {
 constexpr int kNoallocBlocks = 4096;
 constexpr long long kNoallocChunk = 65536;
 constexpr int kThreads = 256;
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_mean_scratch[kNoallocBlocks];
-
-double *g_scratch_addr[kMaxDevices] = {};
-std::mutex g_setup_mutex;
 
 __device__ double block_sum_na(double v) {
   __shared__ double sh[kThreads / 32];
@@ -72,18 +74,12 @@ __global__ void k_mean_finish_na(const double *scratch, int blocks, long long n,
   if (threadIdx.x == 0) *out = s / (double)n;
 }
 
-// device address of the scratch array on the current device (once per device)
-int scratch_for_current_device(double **out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return IH_ERR_CUDA;
-  if (dev < 0 || dev >= kMaxDevices) return IH_ERR_ARG;
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[dev]) {
-    void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_mean_scratch) != cudaSuccess || !p) return IH_ERR_CUDA;
-    g_scratch_addr[dev] = static_cast<double *>(p);
-  }
-  *out = g_scratch_addr[dev];
+// device address of the scratch array in the current context (looked up on
+// every call: a plain table lookup once the module is loaded there)
+int scratch_for_current_context(double **out) {
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_mean_scratch) != cudaSuccess || !p) return IH_ERR_CUDA;
+  *out = static_cast<double *>(p);
   return IH_OK;
 }
 
@@ -97,14 +93,14 @@ int ih_mean_dev_noalloc(const double *f_dev, size_t n, double *out_dev, void *st
   if (!f_dev || !out_dev || n == 0) return IH_ERR_ARG;
   if (n > ih_mean_dev_noalloc_max_n()) return IH_ERR_TOO_LARGE;
   double *scratch = nullptr;
-  int st = scratch_for_current_device(&scratch);
+  int st = scratch_for_current_context(&scratch);
   if (st != IH_OK) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int blocks = (int)((n + kNoallocChunk - 1) / kNoallocChunk);
   k_mean_partials_na<<<blocks, kThreads, 0, s>>>(f_dev, (long long)n, scratch);
-  if (cudaGetLastError() != cudaSuccess) return IH_ERR_CUDA;
+  if (cudaPeekAtLastError() != cudaSuccess) return IH_ERR_CUDA;
   k_mean_finish_na<<<1, kThreads, 0, s>>>(scratch, blocks, (long long)n, out_dev);
-  if (cudaGetLastError() != cudaSuccess) return IH_ERR_CUDA;
+  if (cudaPeekAtLastError() != cudaSuccess) return IH_ERR_CUDA;
   return IH_OK;
 }
 

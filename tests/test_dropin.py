@@ -10,10 +10,12 @@ from pathlib import Path
 import pytest
 
 from instaheat_gb300 import dropin
+from oracle import ref
 
 HERE = Path(__file__).resolve().parent
 PARAMS = HERE / "dropin"
-REF_SRC = Path(os.environ.get("IH_REFERENCE_SRC", "/root/reference/src"))
+# the reference's sources as oracle/ref.py stages them (unchanged copies)
+REF_SRC = ref.STAGE
 
 # the symbols toolbox.h:15-35, dopri853.h:51 and rk4.h:14 declare
 REFERENCE_SYMBOLS = ["mk_rhs", "prepare_and_save_timeslice", "mk_gradient_squared_and_laplacian",
@@ -68,7 +70,7 @@ def test_dropin_object_exports_reference_symbols(tmp_path):
         assert s in nm, s
 
 
-@pytest.mark.skipif(not (REF_SRC / "main_template.h").exists(), reason="reference tree absent")
+@pytest.mark.skipif(not ref.available(), reason="the reference's sources are not staged")
 def test_dropin_compiles_against_reference_generated_headers(tmp_path):
     """ih_dropin.c against the main.h the reference's configure would make from
     its own parameters.sh (with FFTW/HDF5 type stubs): syntax-only."""
@@ -104,3 +106,42 @@ def test_host_without_gpu_exits_with_the_error(tmp_path):
                        capture_output=True, text=True, timeout=120)
     assert r.returncode != 0
     assert "CUDA" in r.stderr or "CUDA" in r.stdout, (r.stdout, r.stderr)
+
+
+def _relinked(name="parameters_dopri853.sh"):
+    from instaheat_gb300 import build as libbuild
+    p = dropin.read_parameters(PARAMS / name)
+    keys = {k: v for k, v in p.items()
+            if k in ref.DEFAULTS and k not in ("DATAPATH", "INITIAL_DATAPATH")}
+    params = ref.config(**keys)
+    exe = ref.build_dropin(params, libbuild.build(), dropin.HERE / "ih_dropin.c",
+                           dropin.ROOT / "include")
+    return p, params, exe
+
+
+@pytest.mark.skipif(not ref.available(), reason="the reference's sources are not staged")
+def test_reference_program_relinks_with_the_dropin():
+    """The reference's own main.c, setup.c and io.c, unchanged, link against
+    ih_dropin.o + libinstaheat_gpu.so in place of toolbox.o, dopri853.o,
+    dopri853_constants.o and rk4.o: main comes from the reference, the
+    toolbox/stepper symbols from the drop-in, nothing is left undefined."""
+    _, _, exe = _relinked()
+    syms = subprocess.run(["nm", str(exe)], capture_output=True, text=True, check=True).stdout
+    defined = {ln.split()[-1] for ln in syms.splitlines() if len(ln.split()) == 3}
+    for s in REFERENCE_SYMBOLS + ["main", "allocate_and_init_all", "h5_create_empty_by_path",
+                                  "save"]:
+        assert s in defined, s
+    assert "ihref_main" not in defined and "perform_step" not in defined
+
+
+@pytest.mark.skipif(not ref.available(), reason="the reference's sources are not staged")
+def test_relinked_program_without_gpu_exits_with_the_error(oracle_mod):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    p, params, exe = _relinked()
+    o = oracle_mod.Oracle(n=(int(p["GRIDPOINTS_X"]),) * 3, bins=int(p["POWER_SPECTRUM_BINS"]))
+    r, _ = ref.run_program(exe, o.ic(seed=11, amp=1e-3, psi=False), exe.parent, timeout=120)
+    assert r.returncode != 0
+    assert "Read initial data from file." in r.stdout  # the reference's set-up ran
+    assert "CUDA" in r.stderr, r.stderr

@@ -12,105 +12,11 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+import dropin_expected as X
 from instaheat_gb300 import dropin
 
 PARAMS = Path(__file__).resolve().parent / "dropin"
 pytestmark = pytest.mark.gpu
-
-
-def _initial_state(o, seed=11):
-    """phi, dphi from the seeded generator; psi, dpsi zero (the host solves
-    them from the constraints); a = 1."""
-    return o.ic(seed=seed, amp=1e-3, psi=False)
-
-
-def _diag_slice(o, d):
-    return {"phi_power_spectrum": d.phi_ps.copy(), "psi_power_spectrum": d.psi_ps.copy(),
-            "rho_power_spectrum": d.rho_ps.copy(), "gravitational_wave_spectrum": d.gw.copy(),
-            "constraints": d.cstr, "phi_summary": d.smry[0], "dphi_summary": d.smry[1],
-            "psi_summary": d.smry[2], "dpsi_summary": d.smry[3], "rho_summary": d.smry[4],
-            "pressure_summary": d.smry[5]}
-
-
-def _record(out, o, f, t, d, rho):
-    s = _diag_slice(o, d)
-    s["time"] = np.array([t])
-    s["a"] = np.array([f[-1]])
-    n = o.n
-    s["phi"] = f[: o.N].reshape(n)[::2, ::2, ::2].ravel()
-    s["rho"] = rho.reshape(n)[::2, ::2, ::2].ravel()
-    for k, v in s.items():
-        out.setdefault(k, []).append(np.asarray(v, dtype=np.float64))
-
-
-def _expected_dopri(oracle_mod, p):
-    """run_dopri853 + save() + wrap-up (dopri853.c:112-233, io.c:494-616)
-    restated over the oracle."""
-    n = (int(p["GRIDPOINTS_X"]),) * 3
-    o = oracle_mod.Oracle(n=n, bins=int(p["POWER_SPECTRUM_BINS"]))
-    f = _initial_state(o)
-    o.initial_psi(f)
-    cfg = oracle_mod.default_cfg(float(p["RELATIVE_TOLERANCE"]), float(p["ABSOLUTE_TOLERANCE"]),
-                                 float(p["MAX_DT_HUBBLE_FRACTION"]))
-    skip = int(p["TIME_STEP_SKIPS"])
-    tf, dt = float(p["FINAL_TIME"]), float(p["DELTA_T"])
-    out = {}
-    d = oracle_mod.DiagOutput(o.bins)
-    _, f_filt = o.rhs(f, filter=1, output=1, diag=d)
-    _record(out, o, f_filt, 0.0, d, o.field_array("rho"))
-    st, df = o.dopri_init(f, cfg, 0.0, dt)
-    t, n_stp, n_ok, n_bad = 0.0, 0, 0, 0
-    while True:
-        if t + dt * 1.0001 > tf:
-            dt = tf - t
-        want = (n_stp + 1) % skip == 0
-        d = oracle_mod.DiagOutput(o.bins)
-        assert o.dopri_step(f, df, cfg, st, dt, d if want else None) == 0
-        if st.dt_did == dt:
-            n_ok += 1
-        else:
-            n_bad += 1
-        t = st.t
-        if want:
-            _record(out, o, f, t, d, o.field_array("rho"))
-        if t >= tf:
-            break
-        dt = st.dt_next
-        n_stp += 1
-    # the wrap-up adds a last slice only while the output buffer is partly
-    # filled (dopri853.c:209-212: index != 0)
-    saves = len(out["time"])
-    if saves % int(p["WRITE_OUT_BUFFER_NUMBER"]) != 0 and out["time"][-1][0] < t:
-        d = oracle_mod.DiagOutput(o.bins)
-        _, f = o.rhs(f, t=t, filter=1, output=1, diag=d)
-        _record(out, o, f, t, d, o.field_array("rho"))
-    steps = {"steps_total": n_stp, "steps_ok": n_ok, "steps_bad": n_bad}
-    return {k: np.array(v) for k, v in out.items()}, steps, f
-
-
-def _expected_rk4(oracle_mod, p):
-    """run_rk4 (rk4.c:27-132) restated over the oracle."""
-    n = (int(p["GRIDPOINTS_X"]),) * 3
-    o = oracle_mod.Oracle(n=n, bins=int(p["POWER_SPECTRUM_BINS"]))
-    f = _initial_state(o)
-    o.initial_psi(f)
-    skip = int(p["TIME_STEP_SKIPS"])
-    tf, dt = float(p["FINAL_TIME"]), float(p["DELTA_T"])
-    out, t, nt = {}, 0.0, 0
-    while t < tf:
-        if t + dt * 1.0001 > tf:
-            dt = tf - t
-        if nt % skip == 0:
-            d = oracle_mod.DiagOutput(o.bins)
-            _, f_filt = o.rhs(f, t=t, filter=1, output=1, diag=d)
-            _record(out, o, f_filt, t, d, o.field_array("rho"))
-        o.rk4_step(f, t, dt)
-        t += dt
-        nt += 1
-    d = oracle_mod.DiagOutput(o.bins)
-    _, f = o.rhs(f, t=t, filter=1, output=1, diag=d)
-    _record(out, o, f, t, d, o.field_array("rho"))
-    return {k: np.array(v) for k, v in out.items()}, f
 
 
 def _run_host(tmp_path, name, oracle_mod):
@@ -119,7 +25,7 @@ def _run_host(tmp_path, name, oracle_mod):
     exe = dropin.build_host(p, tmp_path / "host")
     n = (int(p["GRIDPOINTS_X"]),) * 3
     o = oracle_mod.Oracle(n=n, bins=int(p["POWER_SPECTRUM_BINS"]))
-    _initial_state(o).tofile(tmp_path / "init.bin")
+    X.initial_state(o).tofile(tmp_path / "init.bin")
     r = subprocess.run([str(exe), str(tmp_path / "init.bin"), str(tmp_path / "out.ihc"),
                         str(tmp_path / "final.bin")], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
@@ -141,7 +47,7 @@ def _compare_series(got, exp):
 
 def test_run_dopri853_through_the_dropin(tmp_path, oracle_mod):
     p, got, final = _run_host(tmp_path, "parameters_dopri853.sh", oracle_mod)
-    exp, steps, f_exp = _expected_dopri(oracle_mod, p)
+    exp, steps, f_exp = X.expected_dopri(oracle_mod, p)
     _compare_series(got, exp)
     for k, v in steps.items():
         assert got[k][0] == v, k
@@ -155,57 +61,14 @@ def test_run_dopri853_through_the_dropin(tmp_path, oracle_mod):
 
 def test_run_rk4_through_the_dropin(tmp_path, oracle_mod):
     p, got, final = _run_host(tmp_path, "parameters_rk4.sh", oracle_mod)
-    exp, f_exp = _expected_rk4(oracle_mod, p)
+    exp, f_exp = X.expected_rk4(oracle_mod, p)
     _compare_series(got, exp)
     assert np.abs(final - f_exp).max() <= 1e-9 * np.abs(f_exp[: 4 * 16 ** 3]).max()
 
 
-def _expected_landing(oracle_mod, p):
-    """run_dopri853 with output landing (IH_OUTPUT_INTERVAL) restated over the
-    oracle: steps shortened to end on multiples of the interval, slices there."""
-    n = (int(p["GRIDPOINTS_X"]),) * 3
-    o = oracle_mod.Oracle(n=n, bins=int(p["POWER_SPECTRUM_BINS"]))
-    f = _initial_state(o)
-    o.initial_psi(f)
-    cfg = oracle_mod.default_cfg(float(p["RELATIVE_TOLERANCE"]), float(p["ABSOLUTE_TOLERANCE"]),
-                                 float(p["MAX_DT_HUBBLE_FRACTION"]))
-    tf, dt = float(p["FINAL_TIME"]), float(p["DELTA_T"])
-    interval = float(p["IH_OUTPUT_INTERVAL"])
-    out = {}
-    d = oracle_mod.DiagOutput(o.bins)
-    _, f_filt = o.rhs(f, filter=1, output=1, diag=d)
-    _record(out, o, f_filt, 0.0, d, o.field_array("rho"))
-    st, df = o.dopri_init(f, cfg, 0.0, dt)
-    t, n_out = 0.0, 1
-    t_next = n_out * interval
-    while True:
-        if t + dt * 1.0001 > tf:
-            dt = tf - t
-        want = False
-        if t_next < tf and t + dt * 1.0001 > t_next:
-            dt = t_next - t
-            want = True
-        d = oracle_mod.DiagOutput(o.bins)
-        assert o.dopri_step(f, df, cfg, st, dt, d if want else None) == 0
-        t = st.t
-        if want and abs(t - t_next) <= 1e-12 * max(1.0, abs(t_next)):
-            _record(out, o, f, t, d, o.field_array("rho"))
-            n_out += 1
-            t_next = n_out * interval
-        if t >= tf:
-            break
-        dt = st.dt_next
-    saves = len(out["time"])
-    if saves % int(p["WRITE_OUT_BUFFER_NUMBER"]) != 0 and out["time"][-1][0] < t:
-        d = oracle_mod.DiagOutput(o.bins)
-        _, f = o.rhs(f, t=t, filter=1, output=1, diag=d)
-        _record(out, o, f, t, d, o.field_array("rho"))
-    return {k: np.array(v) for k, v in out.items()}
-
-
 def test_run_dopri853_output_landing(tmp_path, oracle_mod):
     p, got, _ = _run_host(tmp_path, "parameters_landing.sh", oracle_mod)
-    exp = _expected_landing(oracle_mod, p)
+    exp = X.expected_landing(oracle_mod, p)
     times = got["time"][:, 0]
     # slices at 0, 0.02 and 0.04 (landed); the third fills the buffer of three,
     # so the wrap-up adds no slice at 0.05 (dopri853.c:209-212)
@@ -213,66 +76,48 @@ def test_run_dopri853_output_landing(tmp_path, oracle_mod):
     _compare_series(got, exp)
 
 
-def _expected_dense(oracle_mod, p):
-    """run_dopri853 with dense output (IH_OUTPUT_INTERVAL + IH_DENSE_OUTPUT)
-    restated over the oracle: the controller's steps; a step that contains
-    output times is redone from its start with the oracle's continuous
-    extension at those times, whose states pass through the output RHS."""
-    n = (int(p["GRIDPOINTS_X"]),) * 3
-    o = oracle_mod.Oracle(n=n, bins=int(p["POWER_SPECTRUM_BINS"]))
-    f = _initial_state(o)
-    o.initial_psi(f)
-    cfg = oracle_mod.default_cfg(float(p["RELATIVE_TOLERANCE"]), float(p["ABSOLUTE_TOLERANCE"]),
-                                 float(p["MAX_DT_HUBBLE_FRACTION"]))
-    tf, dt = float(p["FINAL_TIME"]), float(p["DELTA_T"])
-    interval = float(p["IH_OUTPUT_INTERVAL"])
-    out = {}
-    d = oracle_mod.DiagOutput(o.bins)
-    _, f_filt = o.rhs(f, filter=1, output=1, diag=d)
-    _record(out, o, f_filt, 0.0, d, o.field_array("rho"))
-    st, df = o.dopri_init(f, cfg, 0.0, dt)
-    t, n_out = 0.0, 1
-    t_next = n_out * interval
-    dense_steps = 0
-    while True:
-        if t + dt * 1.0001 > tf:
-            dt = tf - t
-        f0, df0, st0, t0 = f.copy(), df.copy(), type(st).from_buffer_copy(st), t
-        assert o.dopri_step(f, df, cfg, st, dt) == 0
-        t = st.t
-        times = []
-        while t_next < tf and t_next <= t:
-            times.append(t_next)
-            n_out += 1
-            t_next = n_out * interval
-        if times:
-            h = st.dt_did
-            f[:], df[:] = f0, df0
-            st = type(st).from_buffer_copy(st0)
-            rc, dense = o.dopri_step_dense(f, df, cfg, st, dt, [(x - t0) / h for x in times])
-            assert rc == 0 and st.dt_did == h
-            dense_steps += 1
-            for x, fd in zip(times, dense):
-                d = oracle_mod.DiagOutput(o.bins)
-                _, fd = o.rhs(fd, t=x, filter=1, output=1, diag=d)
-                _record(out, o, fd, x, d, o.field_array("rho"))
-        if t >= tf:
-            break
-        dt = st.dt_next
-    saves = len(out["time"])
-    if saves % int(p["WRITE_OUT_BUFFER_NUMBER"]) != 0 and out["time"][-1][0] < t:
-        d = oracle_mod.DiagOutput(o.bins)
-        _, f = o.rhs(f, t=t, filter=1, output=1, diag=d)
-        _record(out, o, f, t, d, o.field_array("rho"))
-    assert dense_steps >= 1
-    return {k: np.array(v) for k, v in out.items()}
-
-
 def test_run_dopri853_dense_output(tmp_path, oracle_mod):
     p, got, _ = _run_host(tmp_path, "parameters_dense.sh", oracle_mod)
-    exp = _expected_dense(oracle_mod, p)
+    exp = X.expected_dense(oracle_mod, p)
     times = got["time"][:, 0]
     # slices at 0, 0.02 and 0.04 from the continuous extension (the steps are
     # not shortened); the buffer of three is full, so the wrap-up adds none
     np.testing.assert_allclose(times, [0.0, 0.02, 0.04], atol=1e-14)
     _compare_series(got, exp)
+
+
+@pytest.mark.parametrize("name", ["parameters_dopri853.sh", "parameters_rk4.sh"])
+def test_reference_program_relinked_with_the_dropin(oracle_mod, name):
+    """The reference's own main.c, setup.c and io.c, unchanged, relinked with
+    ih_dropin.o + libinstaheat_gpu.so (oracle/ref.py build_dropin), against
+    the reference program itself (oracle/_ref, CPU) on the same .dat initial
+    data: every recorded dataset slice by slice, the step counters and the
+    followup snapshot."""
+    from oracle import ref
+    if not ref.available():
+        pytest.skip("the reference's sources are not staged (oracle/_ref/src)")
+    from instaheat_gb300 import build as libbuild
+    p = dropin.read_parameters(PARAMS / name)
+    keys = {k: v for k, v in p.items()
+            if k in ref.DEFAULTS and k not in ("DATAPATH", "INITIAL_DATAPATH")}
+    params = ref.config(**keys)
+    exe = ref.build_dropin(params, libbuild.build(), dropin.HERE / "ih_dropin.c",
+                           dropin.ROOT / "include")
+    n = (int(p["GRIDPOINTS_X"]),) * 3
+    o = oracle_mod.Oracle(n=n, bins=int(p["POWER_SPECTRUM_BINS"]))
+    f0 = X.initial_state(o)
+    r, got = ref.run_program(exe, f0, exe.parent, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    want = ref.run(ref.build(params), "main", f0)["h5"]
+    series = [k for k, v in want.items()
+              if isinstance(v, np.ndarray) and k in X.SERIES]
+    assert series, sorted(want)
+    _compare_series({k: got[k] for k in series}, {k: want[k] for k in series})
+    for k in ("steps_total", "steps_ok", "steps_bad", "gridpoints_internal", "tolerances",
+              "strides_space", "mass", "filter", "gravitational_waves"):
+        if k in want:
+            assert got[k].tolist() == want[k].tolist(), k
+    if "followup" in want:
+        sc = np.abs(want["followup"][:4 * o.N]).max()
+        assert np.abs(got["followup"] - want["followup"]).max() <= 1e-9 * sc
+    assert got["method"] == want["method"] == b"hyperbolic"

@@ -593,3 +593,58 @@ def test_dopri853_radix3_steps_parity(gpu_mod, oracle_mod):
         dt_g, dt_o = info.dt_next, st.dt_next
     errs = seg_rel_err(ctx.get_state(), fo, o.N, o.Next)
     assert max(errs.values()) < 1e-11, errs
+
+
+@pytest.mark.parametrize("n", [(64, 64, 64), (256, 256, 256)])
+def test_rhs_f64_parity_configured_sizes(gpu_mod, oracle_mod, n):
+    """Plain FP64 mk_rhs at the configured grid sizes (64^3: the FP64
+    DOPRI853 workload; 256^3: the denominator of the headline metric), filter
+    and output on, within 1e-11 of each segment's largest magnitude."""
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o)
+    d = oracle_mod.DiagOutput(o.bins)
+    r_ref, f_ref = o.rhs(f, filter=1, output=1, diag=d)
+    r_gpu, f_gpu = ctx.mk_rhs(f, filter=1, output=1)
+    errs = seg_rel_err(r_gpu, r_ref, o.N, o.Next)
+    assert max(errs.values()) < 1e-11, errs
+    assert np.abs(f_gpu - f_ref).max() < 1e-13
+    g = ctx.output()
+    for k in ("phi_ps", "psi_ps", "rho_ps", "gw"):
+        ref = getattr(d, k)
+        assert np.abs(g[k] - ref).max() <= 1e-10 * np.abs(ref).max(), k
+    atol = np.array([1e-26, 1e-14, 1e-26, 1e-14])
+    assert np.all(np.abs(g["cstr"] - d.cstr) <= 1e-6 * np.abs(d.cstr) + atol), (g["cstr"], d.cstr)
+    ctx.close()
+    o.close()
+
+
+def test_dopri853_f64_to_t10(gpu_mod, oracle_mod):
+    """32^3 FP64 DOPRI853 at rtol = atol = 1e-10 from t = 0 to t = 10/m (the
+    reference's run loop: the last step clamped onto tf): the same accepted
+    step sequence as the oracle, fields within 1e-9 of each segment's largest
+    magnitude, the constraint residuals of the final slice within 1e-6."""
+    n = (32, 32, 32)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
+    o = oracle_mod.Oracle(n=n)
+    f = o.ic(seed=21, amp=1e-3)
+    cfg_o = oracle_mod.default_cfg(1e-10, 1e-10, 1e-2)
+    ctx.set_state(f)
+    ctx.dopri_init(gpu_mod.dopri_cfg(1e-10, 1e-10, max_dt_hubble_fraction=1e-2), 0.0, 1e-3)
+    n_g, log_g = ctx.dopri_run(10.0, 100000, 100000)
+    fo = f.copy()
+    st, dfo = o.dopri_init(fo, cfg_o, 0.0, 1e-3)
+    n_o, log_o = o.dopri_run(fo, dfo, cfg_o, st, 10.0, 100000, 100000)
+    assert n_g == n_o and n_o > 100
+    assert ctx.t == 10.0 and st.t == 10.0
+    # accepted t and dt per step (log rows: t, dt, err, accepted)
+    np.testing.assert_allclose(log_g[:, :2], log_o[:, :2], rtol=1e-9)
+    errs = seg_rel_err(ctx.get_state(), fo, o.N, o.Next)
+    assert max(errs.values()) < 1e-9, errs
+    g = ctx.prepare_output()
+    d = oracle_mod.DiagOutput(o.bins)
+    o.rhs(fo, t=10.0, filter=1, output=1, diag=d)
+    np.testing.assert_allclose(g["cstr"], d.cstr, rtol=1e-6, atol=1e-26)
+    np.testing.assert_allclose(g["gw"], d.gw, rtol=1e-8, atol=1e-14 * np.abs(d.gw).max())
+    ctx.close()
+    o.close()

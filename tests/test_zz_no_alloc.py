@@ -43,6 +43,43 @@ def test_noalloc_mean_matches_allocating_entry_point(gpu_mod):
         assert abs(got - x.mean().item()) <= 1e-12 * abs(ref)
 
 
+def test_noalloc_mean_edge_sizes(gpu_mod):
+    # one element, exactly one block's chunk (65536), and one past it (2 blocks)
+    torch = pytest.importorskip("torch")
+    L = _lib(gpu_mod)
+    ctx = gpu_mod.Context(n=(16, 16, 16))
+    out_ref = torch.zeros(1, dtype=torch.float64, device="cuda")
+    out_na = torch.zeros(1, dtype=torch.float64, device="cuda")
+    for n in (1, 65536, 65537, 1, 65537):
+        x = torch.randn(n, dtype=torch.float64, device="cuda") + 3.0
+        torch.cuda.synchronize()
+        assert L.ih_mean_dev(ctx.h, C.c_void_p(x.data_ptr()), n, C.c_void_p(out_ref.data_ptr())) == 0
+        assert L.ih_mean_dev_noalloc(C.c_void_p(x.data_ptr()), n, C.c_void_p(out_na.data_ptr()),
+                                     None) == 0
+        torch.cuda.synchronize()
+        ref, got = out_ref.item(), out_na.item()
+        assert abs(got - ref) <= 1e-13 * abs(ref), (n, got, ref)
+
+
+def test_noalloc_mean_on_user_stream(gpu_mod):
+    # the call runs on the caller's stream and returns without waiting
+    torch = pytest.importorskip("torch")
+    L = _lib(gpu_mod)
+    s = torch.cuda.Stream()
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    with torch.cuda.stream(s):
+        x = torch.randn(2_000_003, dtype=torch.float64, device="cuda") - 1.5
+        y = torch.randn(131_073, dtype=torch.float64, device="cuda") + 4.0
+        for i, v in enumerate((x, y)):
+            assert L.ih_mean_dev_noalloc(C.c_void_p(v.data_ptr()), v.numel(),
+                                         C.c_void_p(out.data_ptr() + 8 * i),
+                                         C.c_void_p(s.cuda_stream)) == 0
+    s.synchronize()
+    for i, v in enumerate((x, y)):
+        ref = v.mean().item()
+        assert abs(out[i].item() - ref) <= 1e-12 * abs(ref), (i, out[i].item(), ref)
+
+
 def test_noalloc_mean_rejects_oversize(gpu_mod):
     torch = pytest.importorskip("torch")
     L = _lib(gpu_mod)
