@@ -278,7 +278,11 @@ int ih_dopri853_step(ih_context *c, double dt_try, int want_output,
                      ih_step_info *info);
 /* The run loop (dopri853.c:112-158) to tf or max_steps accepted steps; if
  * log is not NULL, 4 doubles (t, dt_did, err, tries) per accepted step are
- * written up to log_cap steps.  *n_steps receives the accepted steps. */
+ * written up to log_cap steps.  *n_steps receives the accepted steps.  The
+ * run ends with IH_ERR_UNDERFLOW where the reference reports a step-size
+ * underflow: a try shrinking below |t| * DBL_EPSILON (perform_step,
+ * dopri853.c:280-283) or a proposed step at or below dt_min
+ * (MINIMAL_DELTA_T, dopri853.c:150-153; the accepted steps before it stand). */
 int ih_dopri853_run(ih_context *c, double tf, long max_steps, double *log,
                     long log_cap, long *n_steps);
 /* Controller state: dt_next and the number of accepted/rejected steps. */
@@ -394,8 +398,12 @@ int ih_get_step_start_state(ih_context *c, double *f_host);
 int ih_dopri853_set_noise_floor(ih_context *c, double eta);
 /* Diagnostic: with diag on, every try also sums the squared scaled error
  * components per state segment; ih_dopri853_error_breakdown returns the last
- * try's sums [phi, dphi, psi, dpsi, h1+h2, dh1+dh2] x (5th-order, 3rd-order)
- * (the scale factor's share is the remainder of the total). */
+ * try's sums [phi, dphi, psi, dpsi, h1+h2, dh1+dh2] x (S_bhh, S_er): S_bhh
+ * sums (yerr/sk)^2 with yerr from the b - bhh weights (the 3rd-order
+ * estimate, dopri853.c:451-452), S_er sums (yerr2/sk)^2 with the er weights
+ * (the 5th-order estimate, 453-456); error() = dt * S_er / sqrt(Ntot * (S_er
+ * + 0.01 S_bhh)) over all segments (dopri853.c:469-486; the scale factor's
+ * share is the remainder of the totals). */
 int ih_dopri853_diag_enable(ih_context *c, int on);
 int ih_dopri853_error_breakdown(ih_context *c, double *out12);
 

@@ -669,7 +669,13 @@ int ih_dopri853_run(ih_context *h, double tf, long max_steps, double *log, long 
     }
     if (c->t >= tf) break;
     if (c->n_stp + 1 >= max_steps) break;
-    if (fabs(c->dt_next) <= c->cfg.dt_min) break;
+    if (fabs(c->dt_next) <= c->cfg.dt_min) {
+      // the reference prints "Stepsize underflow" and ends the run
+      // (dopri853.c:150-153); here the caller sees the status
+      c->err = "proposed step size at or below MINIMAL_DELTA_T";
+      status = IH_ERR_UNDERFLOW;
+      break;
+    }
     dt = c->dt_next;
   }
   if (n_steps) *n_steps = accepted;

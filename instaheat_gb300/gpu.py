@@ -172,8 +172,18 @@ def load(build_if_missing: bool = True):
     L.ih_ensemble_dopri_init.argtypes = [vp, C.POINTER(DopriCfg), C.c_double, C.c_double]
     L.ih_ensemble_run.argtypes = [vp, C.c_double, C.c_long, C.POINTER(C.c_long),
                                   C.POINTER(C.c_long)]
+    L.ih_fp64_fma_peak.argtypes = [C.c_int, C.c_int, C.c_int, _dp]
     _lib = L
     return L
+
+
+def fp64_fma_peak(device=0, iters=8192, reps=5) -> float:
+    """Measured FP64 FMA throughput of the GPU in TFLOP/s (ih_fp64_fma_peak)."""
+    v = C.c_double()
+    st = load().ih_fp64_fma_peak(device, iters, reps, C.byref(v))
+    if st != 0:
+        raise IHError(st, "ih_fp64_fma_peak")
+    return v.value
 
 
 MLP_INPUTS = 12

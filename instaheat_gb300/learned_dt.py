@@ -13,8 +13,13 @@ records, after every step, its feature vector (ih_step_features: last four
 log dt, last four log error norms, log a, H, log rms delta phi, log rms
 delta psi).  Training pairs: features after step n -> log dt_{n+1} of FP64.
 
-    python -m instaheat_gb300.learned_dt --n 128,256 --seeds 1,2,3 --t-end 1.0 \\
+    python -m instaheat_gb300.learned_dt --runs 128:1:20:1.0,128:2:10:0.8 --t-end 300 \\
         --out instaheat_gb300/data/dt_mlp.json
+
+Each run is grid:seed:box:phi0 (box L in units of 1/m, phi0 the homogeneous
+field); the logs span the whole run, so the proposer sees the early phase
+(the error controller sets dt) and the late phase (the Hubble-fraction cap
+sets it, dopri853.c:525-530).
 """
 from __future__ import annotations
 
@@ -30,18 +35,18 @@ from . import gpu
 DEFAULT_MODEL = Path(__file__).resolve().parent / "data" / "dt_mlp.json"
 
 
-def step_log(n, seed, t_end, rtol=1e-8, device=0, amp=1e-3):
+def step_log(n, seed, t_end, rtol=1e-8, device=0, amp=1e-3, L=20.0, phi0=1.0):
     """(X, Y, info) for one realization: mixed-form features replaying FP64."""
-    c64 = gpu.Context(n=(n,) * 3, precision=gpu.PREC_F64, device=device)
-    c64.ic(seed=seed, amp=amp)
+    c64 = gpu.Context(n=(n,) * 3, L=(L,) * 3, precision=gpu.PREC_F64, device=device)
+    c64.ic(seed=seed, amp=amp, phi0=phi0)
     c64.dopri_init(gpu.dopri_cfg(rtol, rtol), 0.0, 1e-3)
     t0 = time.perf_counter()
     steps, log = c64.dopri_run(t_end, log_cap=1_000_000)
     w64 = time.perf_counter() - t0
     c64.close()
     dts = log[:, 1]
-    cm = gpu.Context(n=(n,) * 3, precision=gpu.PREC_MIXED, device=device)
-    cm.ic(seed=seed, amp=amp)
+    cm = gpu.Context(n=(n,) * 3, L=(L,) * 3, precision=gpu.PREC_MIXED, device=device)
+    cm.ic(seed=seed, amp=amp, phi0=phi0)
     cm.dopri_init(gpu.dopri_cfg(rtol, rtol), 0.0, 1e-3)
     X, Y = [], []
     replayed = 0
@@ -55,7 +60,8 @@ def step_log(n, seed, t_end, rtol=1e-8, device=0, amp=1e-3):
             Y.append(np.log(dts[k + 1]))
     cm.close()
     return (np.array(X, dtype=np.float32).reshape(-1, gpu.MLP_INPUTS), np.array(Y, dtype=np.float32),
-            {"n": n, "seed": seed, "steps_f64": int(steps), "replayed": replayed, "wall_f64_s": w64})
+            {"n": n, "seed": seed, "L": L, "phi0": phi0, "t_end": t_end, "steps_f64": int(steps),
+             "replayed": replayed, "wall_f64_s": w64})
 
 
 def fit(X, Y, device=0, iters=3000, lr=3e-3, seed=1):
@@ -138,6 +144,8 @@ def main(argv=None):
     ap.add_argument("--eval-t", type=float, default=0.5)
     ap.add_argument("--n", default="128,256")
     ap.add_argument("--seeds", default="1,2,3")
+    ap.add_argument("--runs", default=None,
+                    help="grid:seed:box:phi0 entries (comma-separated); overrides --n/--seeds")
     ap.add_argument("--t-end", type=float, default=1.0)
     ap.add_argument("--iters", type=int, default=3000)
     ap.add_argument("--lr", type=float, default=3e-3)
@@ -147,13 +155,18 @@ def main(argv=None):
         print(json.dumps(evaluate(args.eval_n, args.eval_seed, args.eval_t, args.out)), flush=True)
         return
     Xs, Ys, infos = [], [], []
-    for n in [int(x) for x in args.n.split(",")]:
-        for s in [int(x) for x in args.seeds.split(",")]:
-            X, Y, info = step_log(n, s, args.t_end)
-            print(json.dumps(info), flush=True)
-            Xs.append(X)
-            Ys.append(Y)
-            infos.append(info)
+    if args.runs:
+        runs = [(int(a), int(b), float(c), float(d))
+                for a, b, c, d in (r.split(":") for r in args.runs.split(","))]
+    else:
+        runs = [(int(n), int(sd), 20.0, 1.0) for n in args.n.split(",")
+                for sd in args.seeds.split(",")]
+    for n, sd, L, phi0 in runs:
+        X, Y, info = step_log(n, sd, args.t_end, L=L, phi0=phi0)
+        print(json.dumps(info), flush=True)
+        Xs.append(X)
+        Ys.append(Y)
+        infos.append(info)
     X = np.concatenate(Xs)
     Y = np.concatenate(Ys)
     mlp, hist = fit(X, Y, iters=args.iters, lr=args.lr)

@@ -265,6 +265,20 @@ def write_dat(path, field: np.ndarray, N: int, n: tuple):
             fh.write(f"{i} {j} {k} {row[0]:.17g} {row[1]:.17g} {row[2]:.17g} {row[3]:.17g}\n")
 
 
+def write_h5rec(path, datasets: dict):
+    """A file in the HDF5 recorder's format (rank-1 double datasets), e.g.
+    {"followup": state, "time": [t]} for the reference's IC_FROM_H5_FILE
+    restart (io.c:754-788)."""
+    with open(path, "wb") as fh:
+        fh.write(b"IHH5REC1")
+        for name, v in datasets.items():
+            a = np.ascontiguousarray(np.asarray(v, dtype="<f8").reshape(-1))
+            nb = name.encode()
+            fh.write(struct.pack("<I", len(nb)) + nb + struct.pack("<II", 0, 1))
+            fh.write(struct.pack("<QQ", a.size, a.nbytes))
+            fh.write(a.tobytes())
+
+
 def read_h5rec(path) -> dict:
     """The HDF5 recorder's file (ref_shim/ih_ref_shim.c): name -> array
     (rank-2 datasets as (rows, dim), rank-1 as (n,)) or bytes (strings)."""
@@ -320,7 +334,11 @@ def _child(build_dir: Path, work: Path):
     params = json.loads((build_dir / "params.json").read_text())
     n = tuple(int(params[f"GRIDPOINTS_{a}"]) for a in "XYZ")
     N = n[0] * n[1] * n[2]
-    write_dat(work / params["INITIAL_DATAPATH"], inp["state"], N, n)
+    if job.get("ic") == "h5":
+        write_h5rec(work / params["INITIAL_DATAPATH"],
+                    {"followup": inp["state"], "time": [float(job.get("t0", 0.0))]})
+    else:
+        write_dat(work / params["INITIAL_DATAPATH"], inp["state"], N, n)
     res = {}
     kind = job["kind"]
     if kind == "main":
@@ -340,7 +358,7 @@ def _child(build_dir: Path, work: Path):
     field, dfield = arr("field"), arr("dfield")
     res["init_field"] = field.copy()
     res["init_dfield"] = dfield.copy()
-    if job.get("set_state", True):
+    if job.get("set_state", job.get("ic") != "h5"):
         field[:] = inp["state"]
     flags = _Flags.in_dll(L, "evo_flags")
     if kind == "rhs":
@@ -385,6 +403,41 @@ def _child(build_dir: Path, work: Path):
         L.run_rk4()
         res["field"] = field.copy()
         res["t"] = np.array(L.ihref_time())
+    elif kind == "bench":
+        # run_dopri853's prologue from the state the reference read, steps
+        # to settle_t untimed, then `steps` perform_step calls timed one by
+        # one (wall clock around each call; the reference is single-process
+        # OpenMP code)
+        import time as _time
+        L.ihref_set_time(L.ihref_time(), 1.0e30, float(job["dt0"]))
+        L.ihref_dopri_begin.restype = None
+        L.ihref_dopri_step.argtypes = [C.c_double, C.POINTER(C.c_double)]
+        L.ihref_dopri_step.restype = C.c_int
+        calls = C.c_size_t.in_dll(L, "mon")  # monitor.calls_rhs, its first member
+        L.ihref_dopri_begin()
+        info = (C.c_double * 5)()
+        dt = float(job["dt0"])
+        settle = 0
+        while L.ihref_time() < float(job.get("settle_t", -1.0)):
+            if L.ihref_dopri_step(dt, info):
+                raise RuntimeError("step-size underflow while settling")
+            dt = info[2]
+            settle += 1
+        rows = []
+        for _ in range(int(job["steps"])):
+            c0 = calls.value
+            t0 = _time.perf_counter()
+            st = L.ihref_dopri_step(dt, info)
+            sec = _time.perf_counter() - t0
+            # each try is 11 RHS (try_step), the accepted step adds one
+            rows.append([info[0], info[1], sec, (calls.value - c0 - 1) / 11.0, st])
+            if st:
+                break
+            dt = info[2]
+        res["rows"] = np.array(rows)
+        res["settle_steps"] = np.array(settle)
+        res["dt_next"] = np.array(dt)
+        L.ihref_dopri_end()
     elif kind == "init":
         pass
     else:
@@ -398,7 +451,10 @@ def run(build_dir, kind: str, state: np.ndarray, workdir=None, timeout=None, **j
     Ntot-double initial state in the reference layout (its phi, dphi, psi,
     dpsi go into the .dat file; with set_state (default) the whole array
     replaces ``field`` after initialisation).  Returns the arrays the job
-    read back; with a recorder file, its datasets under ``"h5"``."""
+    read back; with a recorder file, its datasets under ``"h5"``.  With
+    ic="h5" (builds with INITIAL_CONDITIONS = IC_FROM_H5_FILE) the state and
+    the time t0 reach the reference as a follow-up file instead (binary, fast
+    at any size), read by its own h5_read_followup."""
     build_dir = Path(build_dir)
     own = workdir is None
     work = Path(tempfile.mkdtemp(prefix="ihref_")) if own else Path(workdir)

@@ -31,7 +31,9 @@ def load_helper(ref_root: Path):
 
 
 def main():
-    ref_root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_flrw_golden.py /path/to/InstaHeat")
+    ref_root = Path(sys.argv[1])
     mod = load_helper(ref_root)
     cases = []
     for phi0 in (1.0, 0.8, 1.2):

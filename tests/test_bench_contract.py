@@ -5,7 +5,7 @@ transforms x (N + Next) values read and written plus the result write,
 15 (N + Next) values; per DOPRI853 step 12 RHS evaluations and 72 Ntot values
 of stage combinations (61 stage-input reads, 1 post-step read, 9 final reads,
 1 write): 63.1 GB in FP32 at 256^3, a 9.3 ms floor at the measured copy peak.
-The committed bench record (profiles/bench_256_mixed_learned.json, a run of
+The committed bench record (profiles/bench_256.json, the line of a run of
 this bench.py on a GB300) carries every key of the line's contract."""
 import importlib.util
 import json
@@ -34,7 +34,7 @@ def test_step_bytes_and_floor():
 
 
 def test_committed_bench_record_has_the_contract_keys():
-    d = json.loads((ROOT / "profiles" / "bench_256_mixed_learned.json").read_text())
+    d = json.loads((ROOT / "profiles" / "bench_256.json").read_text())
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
               "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
               "gpu_launches", "e2e", "roofline", "clocks"):
@@ -55,14 +55,21 @@ def test_committed_bench_record_has_the_contract_keys():
     for k in ("sm_mhz", "sm_max_mhz", "reasons"):
         assert k in c, k
     acc = d["accuracy_vs_f64"]
-    assert acc["within_1pct"] is True and acc["gw_max_rel_diff"] < 0.01
+    assert acc["t_end"] >= 10 and acc["within_1pct"] is True and acc["gw_max_rel_diff"] < 0.01
+    cpu = d["cpu_baseline"]
+    for k in ("value", "unit", "cores", "kind", "sample", "ms_per_step", "dt_per_step", "gpu_dt"):
+        assert k in cpu, k
+    assert cpu["kind"] in ("reference", "port") and cpu["cores"] >= 1
+    # the CPU arm starts from the GPU arm's state with the GPU arm's step size
+    assert cpu["dt_per_step"][0] == cpu["gpu_dt"]
+    assert d["f64"]["roofline"]["fp64"]["peak_source"] == "measured"
 
 
 def test_f64_form_bounds():
     """The FP64 form against both of its bounds at 256^3: 126.1 GB per step
     against HBM, 1.54e11 flops against the FP64 pipe -- the pipe binds."""
     b = _bench()
-    r = b.f64_roofline(274.0, 6778.3, "measured")
+    r = b.f64_roofline(274.0, 6778.3, "measured", 1.25, "measured")
     assert r["hbm"]["bytes_per_step"] == 2 * 63_059_263_776
     assert abs(r["fp64"]["flops_per_step"] - 1.5443e11) < 1e8
     assert abs(r["fp64"]["floor_ms_per_step"] - 123.5) < 0.5
