@@ -244,7 +244,8 @@ def bench_form(gpu, precision, device, seed, steps, warmup, profile=False, clock
                                    (ENGINE_NAMES[e] for e in ctx.engines()[:5])))
                           | {"tensor_x": ("fused" if ctx.engines()[5] else "separate"),
                              "z_fused": ("wide rows" if ctx.engines()[6] else "warp rows"),
-                             "gw_yx_slab": ctx.engines()[7]},
+                             "gw_yx_slab": ctx.engines()[7],
+                             "gw_planes": bool(ctx.engines()[8])},
            "fft_autotune": ctx.autotune_report}
     return ctx, res
 
@@ -748,7 +749,8 @@ def main():
     ctx.close()
     f64 = None
     if not args.no_f64:
-        c64, f64 = bench_form(gpu, gpu.PREC_F64, device, seed, max(2, min(steps, 3)), 3)
+        c64, f64 = bench_form(gpu, gpu.PREC_F64, device, seed, max(2, min(steps, 3)), 3,
+                              profile=True)
         c64.close()
     # whole-job figures (max time over ranks, sum of m*t)
     ms = dist.reduce(mixed["ms"], "max")
@@ -807,9 +809,12 @@ def main():
         if f64:
             f64v = f64["mt"] / (f64["ms"] / 1e3)
             ms64 = f64["ms"] / max(1, min(steps, 3))
+            n64 = max(1, min(steps, 3))
             line["f64"] = {"value": f64v, "unit": UNIT, "ms_per_step": ms64,
                            "dt_next": f64["dt_next"],
-                           "roofline": f64_roofline(ms64, peak, peak_src, fp64, fp64_src)}
+                           "roofline": f64_roofline(ms64, peak, peak_src, fp64, fp64_src),
+                           "kernels_ms_per_step": {k: v[0] / n64 for k, v in f64["kernels"].items()
+                                                   if v[1]}}
             line["speedup_vs_f64"] = value / f64v
         if acc:
             line["accuracy_vs_f64"] = acc

@@ -180,8 +180,9 @@ int ih_variance_host(ih_context *c, double mean, const double *f_host, size_t n,
  * FFTW_DEFAULT_FLAG, parameters.sh, plays this role there) ----
  * Times every engine variant of the x and y passes, of the fused inverse x
  * pass, of the x and y derivative round trips, of the last tensor x pass and
- * the kz slab widths of the tensor sources' y/x passes of the RHS on the
- * context's scratch spectra and keeps the fastest per pass.  Until it is called the passes use the shared-memory Stockham
+ * the kz slab widths of the tensor sources' y/x passes and, where it
+ * applies, the plane-major tail of the tensor sources (pass 8 below) of the
+ * RHS on the context's scratch spectra and keeps the fastest per pass.  Until it is called the passes use the shared-memory Stockham
  * engine.  Results are identical across variants up to rounding.  The report
  * lists the timings and the choice (valid until the next ih_autotune). */
 int ih_autotune(ih_context *c);
@@ -195,7 +196,11 @@ const char *ih_autotune_report(const ih_context *c);
  * the kz slab width of the forward y and x passes of the six tensor sources
  * (0 = whole arrays, the default; a multiple of 8 up to 64 = y then x pass on
  * one slab of all six at a time, so the slab stays in L2 between the two; it
- * applies with pass 5 = 0);
+ * applies with pass 5 = 0), 8 = the tensor sources plane-major (1: the fused
+ * z pass writes each source as 129 contiguous 256 x 256 kz planes, one
+ * cluster of 8 CTAs transforms a plane along y and x in one pass through
+ * distributed shared memory, and update_h reads the planes; mixed form at
+ * 256^3 only, IH_ERR_ARG elsewhere; 0: the row and column passes);
  * engine IH_FFT_STOCKHAM, IH_FFT_TWOSTEP (register two-step,
  * 128-byte tiles), IH_FFT_TWOSTEP_HALF (64-byte tiles), IH_FFT_PIPELINED
  * (register two-step in persistent CTAs that copy the next tile in with

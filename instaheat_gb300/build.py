@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_lib"
 LIB = OUT / "libinstaheat_gpu.so"
 CU_SOURCES = ["ih_api.cu", "ih_fft.cu", "ih_zwide.cu", "ih_rhs.cu", "ih_stepper.cu", "ih_mlp.cu",
-              "ih_noalloc.cu", "ih_peak.cu"]
+              "ih_noalloc.cu", "ih_peak.cu", "ih_gwplane.cu"]
 HEADERS = ["ih_internal.cuh", "ih_fftcore.cuh", "ih_tensor.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -21,11 +21,13 @@ const char *kernel_kind_name(int k) {
   static const char *names[KK_COUNT] = {
       "k_fft_xy",       "k_fft_zr2c",    "k_fft_zc2r",       "k_fft_x_deriv4_inv",
       "k_fft_xy_rt",    "k_fft_x_tensor", "k_fft_z_rhs_fused", "k_update_h", "k_update_phi_psi", "k_filter_spectra",
-      "k_lincomb",      "k_dopri_final"};
+      "k_lincomb",      "k_dopri_final", "k_gw_plane2d", "k_update_h_plane"};
   return (k >= 0 && k < KK_COUNT) ? names[k] : "unknown";
 }
 
 int kernel_kind_class(int k) {
+  if (k == KK_GW_PLANE) return 0;
+  if (k == KK_UPDATE_H_PLANE) return 1;
   if (k <= KK_Z_RHS_FUSED) return 0;
   if (k <= KK_FILTER) return 1;
   return 2;
@@ -186,6 +188,8 @@ static int create(const ih_params *p, Ctx *c) {
   IH_CUDA(c, cudaMemsetAsync(c->rs, 0, sizeof(RhsScalars), c->stream));
   IH_TRY(dmalloc(c, (void **)&c->diag, sizeof(double) * (4 * g.bins + 128)));
   IH_CUDA(c, cudaMemsetAsync(c->diag, 0, sizeof(double) * (4 * g.bins + 128), c->stream));
+  IH_TRY(dmalloc(c, (void **)&c->waitflag, sizeof(int)));
+  IH_CUDA(c, cudaMemsetAsync(c->waitflag, 0, sizeof(int), c->stream));
   c->hpin_bytes = 4096;
   IH_CUDA(c, cudaMallocHost((void **)&c->hpin, c->hpin_bytes));
   IH_TRY(dmalloc(c, &c->stage_dev, sizeof(double) * (size_t)g.Ntot));
@@ -212,6 +216,7 @@ static void destroy(Ctx *c) {
   if (c->partials) cudaFree(c->partials);
   if (c->rs) cudaFree(c->rs);
   if (c->diag) cudaFree(c->diag);
+  if (c->waitflag) cudaFree(c->waitflag);
   if (c->hpin) cudaFreeHost(c->hpin);
   if (c->stage_dev) cudaFree(c->stage_dev);
   if (c->feat_dev) cudaFree(c->feat_dev);
@@ -500,6 +505,16 @@ const char *ih_autotune_report(const ih_context *h) {
 
 int ih_fft_set_engine(ih_context *h, int pass, int engine) {
   CTX_CHECK(h);
+  if (pass == 8) {  // plane-major tensor sources with the one-pass plane transforms
+    if (engine < 0 || engine > 1) return IH_ERR_ARG;
+    if (engine == 1 && !gw_plane_ok(&h->c)) {
+      h->c.err = "the plane transforms apply to the mixed form at 256^3 with GW on";
+      return IH_ERR_ARG;
+    }
+    h->c.gw_plane = engine;
+    h->c.graph_epoch += 1;
+    return IH_OK;
+  }
   if (pass == 7) {  // kz slab width of the tensor sources' y/x passes
     if (engine < 0 || engine > 64 || engine % 8) return IH_ERR_ARG;
     h->c.gw_slab = engine;
@@ -554,7 +569,8 @@ int ih_graphs_enable(ih_context *h, int on) {
 }
 
 int ih_fft_get_engine(const ih_context *h, int pass) {
-  if (!h || pass < 0 || pass > 7) return -1;
+  if (!h || pass < 0 || pass > 8) return -1;
+  if (pass == 8) return h->c.gw_plane;
   if (pass == 7) return h->c.gw_slab;
   if (pass < 2) return h->c.xy_var[pass];
   if (pass == 5) return h->c.tensor_fused;

@@ -2111,12 +2111,18 @@ struct FusedLaunch {
 
 template <typename T>
 int fft_z_rhs_fused(Ctx *c, const C2<T> *d4, const T *yfl, const double *ysc, T *lap, T *p,
-                    T *rho, C2<T> *s6, int gw, double *partials, int *nblocks_out, int zsrc) {
+                    T *rho, C2<T> *s6, int gw, double *partials, int *nblocks_out, int zsrc,
+                    int plane) {
   const Geom &g = c->g;
   prof_begin(c, KK_Z_RHS_FUSED);
   if (sizeof(T) == 4 && fused_wide_ok(c)) {  // nz = 256, mixed form: the wide-row engine
-    IH_TRY(fused_wide_launch(c, d4, yfl, ysc, lap, p, rho, s6, gw, partials, nblocks_out, zsrc));
+    IH_TRY(fused_wide_launch(c, d4, yfl, ysc, lap, p, rho, s6, gw, partials, nblocks_out, zsrc,
+                             plane));
   } else {
+    if (plane) {
+      c->err = "plane-major tensor sources need the wide-row z pass";
+      return IH_ERR_STATE;
+    }
     IH_TRY(dispatch_len(
         g.h, FusedLaunch<T>{c, d4, yfl, ysc, lap, p, rho, s6, gw, partials, nblocks_out, zsrc},
         false));
@@ -2299,15 +2305,65 @@ static int autotune_t(Ctx *c) {
       }
     }
   }
+  // the tensor sources' tail (y and x transforms, projection and equation of
+  // motion) row by row as chosen above, against the one-pass plane
+  // transforms on plane-major sources
+  c->gw_plane = 0;
+  if (st == IH_OK && sizeof(T) == 4 && gw_plane_ok(c)) {
+    float tail[2] = {0.f, 0.f};
+    bool planes_usable = true;
+    for (int v = 0; v < 2 && st == IH_OK; ++v) {
+      for (int r = 0; r <= reps && st == IH_OK; ++r) {
+        if (r == 1) cudaEventRecord(e0, c->stream);
+        if (v == 1) {
+          st = gw_plane_fft(c, sp);
+          if (st == IH_OK) st = update_h_plane(c, sp, c->y.fl, c->ytmp.fl, c->ytmp.sc);
+          if (st != IH_OK) {  // e.g. no room for a cluster of 8: keep the row passes
+            snprintf(line, sizeof line, "gw planes unavailable (%s); ", c->err.c_str());
+            rep += line;
+            cudaStreamSynchronize(c->stream);
+            cudaGetLastError();
+            planes_usable = false;
+            st = IH_OK;
+            break;
+          }
+        } else if (c->gw_slab > 0 && !c->tensor_fused) {
+          st = fft_gw_yx<T>(c, sp, c->gw_slab);
+          if (st == IH_OK)
+            st = tensor_last_pass(c, sp, c->y.fl, c->ytmp.fl, c->ytmp.sc, nullptr, true);
+        } else {
+          st = fft_xy<T>(c, sp, M, 4, 1, -1);
+          if (st == IH_OK) st = fft_xy<T>(c, sp + 5 * M, M, 2, 1, -1);
+          if (st == IH_OK) st = tensor_last_pass(c, sp, c->y.fl, c->ytmp.fl, c->ytmp.sc, nullptr);
+        }
+      }
+      if (st != IH_OK || !planes_usable) break;
+      cudaEventRecord(e1, c->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&tail[v], e0, e1) != cudaSuccess) {
+        c->err = "autotune: event timing failed";
+        st = IH_ERR_CUDA;
+        break;
+      }
+      tail[v] /= reps;
+    }
+    if (st == IH_OK && planes_usable) {
+      c->gw_plane = tail[1] < tail[0];
+      snprintf(line, sizeof line, "gw tail rows %.1f us, planes %.1f us; ", 1e3 * tail[0],
+               1e3 * tail[1]);
+      rep += line;
+    }
+  }
   c->prof_on = prof;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st != IH_OK) return st;
   snprintf(line, sizeof line,
-           "chosen: x %s, y %s, deriv4-x %s, rt-x %s, rt-y %s, tensor %s, gw-yx slab %d",
+           "chosen: x %s, y %s, deriv4-x %s, rt-x %s, rt-y %s, tensor %s, gw-yx slab %d, "
+           "gw planes %d",
            variant_name(c->xy_var[0]), variant_name(c->xy_var[1]), variant_name(c->d4_var),
            variant_name(c->rt_var[0]), variant_name(c->rt_var[1]),
-           c->tensor_fused ? "fused" : "separate", c->gw_slab);
+           c->tensor_fused ? "fused" : "separate", c->gw_slab, c->gw_plane);
   c->tune_report = rep + line;
   return IH_OK;
 }
@@ -2325,7 +2381,7 @@ int fft_autotune(Ctx *c) {
   template int fft_gw_yx<T>(Ctx *, C2<T> *, int);                                              \
   template int fft_x_deriv4_inv<T>(Ctx *, const C2<T> *, C2<T> *, long long);                   \
   template int fft_z_rhs_fused<T>(Ctx *, const C2<T> *, const T *, const double *, T *, T *,    \
-                                  T *, C2<T> *, int, double *, int *, int);                     \
+                                  T *, C2<T> *, int, double *, int *, int, int);                \
   template int fft_xy_roundtrip<T>(Ctx *, const C2<T> *, C2<T> *, C2<T> *, int);              \
   template int fft_x_tensor<T>(Ctx *, const C2<T> *, const C2<T> *, T *, T *, double *,       \
                                const NextLin *);

@@ -1,0 +1,298 @@
+// ih_gwplane.cu -- the tensor sources' y and x transforms in one pass per
+// kz plane, and the TT projection + tensor equation of motion reading them
+// (mixed form, 256^3).
+//
+// The six S_ij spectra are written by the fused z pass plane-major,
+// S[a][kz][x][y] (each kz plane a contiguous 256 x 256 complex block), so
+// that one plane's forward y and x transforms can run in one read and one
+// write of the plane instead of a y pass and an x pass over whole arrays
+// (half the HBM traffic of the row/column engines on these arrays).
+//
+// k_gw_plane2d: one cluster of 8 CTAs per plane.  CTA r of the cluster
+//   1. loads rows x = 32r .. 32r+31 (64 KB, contiguous) with TMA bulk copies
+//      (cp.async.bulk, completion on an mbarrier; the wait is bounded and
+//      records a timeout in a device flag instead of hanging);
+//   2. transforms each row along y: 16 threads per row, n = t + 16m, a
+//      16-point DFT over m in registers, the twiddle w256^(t a), an exchange
+//      through the row's own shared memory (slots a*16 + (t ^ a): no bank
+//      conflicts), a 16-point DFT over t -- thread a ends with y = a + 16b;
+//   3. after a cluster barrier (every CTA done with its rows) stores each
+//      value into the shared memory of the CTA that owns column y (y / 32)
+//      through distributed shared memory, laid out [x][33] (column tiles,
+//      padded against bank conflicts); a second cluster barrier publishes
+//      the stores;
+//   4. transforms its 32 columns along x the same way, in place, and writes
+//      them back to the plane (one 256-byte run per x row and warp).
+// The exchange reuses the load buffer: after step 2 every thread holds its
+// row's values in registers, so the buffer is free once the cluster has
+// passed the first barrier.  70 KB of shared memory and 512 threads per CTA:
+// two CTAs per SM.
+//
+// k_update_h_plane: update_h (toolbox.c:311-346, 363-397) over tiles of one
+// x row, 32 y and 32 kz: the six sources are read plane-major (256-byte runs
+// along y) into shared memory, the state's tensor segments and the outputs
+// are read and written in the reference layout (runs along kz); each thread
+// then applies the same projection and equation of motion as k_update_h.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ih_internal.cuh"
+#include "ih_fftcore.cuh"
+#include "ih_tensor.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace ih {
+namespace {
+
+constexpr int kP = 256;                  // plane extent along x and y
+constexpr int kCl = 8;                   // CTAs per cluster
+constexpr int kRows = kP / kCl;          // rows (and columns) per CTA: 32
+constexpr int kLd = kRows + 1;           // padded row length of the column tiles
+constexpr int kPlaneThreads = 512;       // 16 threads per row / column
+constexpr int kChunkBytes = kRows * kP * 8;   // 64 KB of rows per CTA
+constexpr int kCopies = 4;               // bulk copies per chunk (16 KB each)
+constexpr long long kWaitLimit = 1LL << 20;   // bounded mbarrier wait (attempts)
+
+struct PlaneSmem {
+  float2 buf[kP * kLd];                  // rows [32][256] on load; column tiles [256][33] after
+  float2 tw[kP];                         // exp(-2 pi i k/256)
+  unsigned long long bar;                // mbarrier of the chunk load
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// global -> this CTA's shared memory, completion counted on bar (16-byte
+// aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes,
+                                          unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// waits for phase `parity` of bar; false after kWaitLimit attempts
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity) {
+  for (long long i = 0; i < kWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// 256-point forward transform of 16 values held by the 16 threads of a line
+// (thread t holds v[m] = x[t + 16m]); `line` is the line's 256 slots with
+// stride `ld` (complex) between consecutive slots.  On return thread t holds
+// v[b] = X[t + 16b].
+__device__ __forceinline__ void line_fft256(float2 (&v)[16], int t, float2 *line, int ld,
+                                            const float2 *tw) {
+  reg_dft<float, 16>(v, tw, 16, -1);
+#pragma unroll
+  for (int a = 1; a < 16; ++a) v[a] = cmul(v[a], tw[t * a]);
+#pragma unroll
+  for (int a = 0; a < 16; ++a) line[(a * 16 + (t ^ a)) * ld] = v[a];
+  __syncwarp();
+#pragma unroll
+  for (int s = 0; s < 16; ++s) v[s] = line[(t * 16 + (s ^ t)) * ld];
+  __syncwarp();
+  reg_dft<float, 16>(v, tw, 16, -1);
+}
+
+// One kz plane of one of the six S_ij spectra per cluster: forward y then x
+// transforms, in place.  spec: the complex spectra of the RHS (slots 0..3
+// and 5, 6 hold the sources), M complex each.
+__global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kPlaneThreads, 2)
+    k_gw_plane2d(float2 *spec, long long M, int mz, const float2 *__restrict__ twg, int *waitflag) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  PlaneSmem &sm = *reinterpret_cast<PlaneSmem *>(smraw);
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const int tid = threadIdx.x;
+  const long long p = blockIdx.x / kCl;          // plane: array a, kz
+  const int a = (int)(p / mz), kz = (int)(p % mz);
+  float2 *plane = spec + (long long)(a < 4 ? a : a + 1) * M + (long long)kz * kP * kP;
+
+  if (tid == 0) {
+    mbar_init(&sm.bar, 1);
+    mbar_expect_tx(&sm.bar, kChunkBytes);
+    const char *src = reinterpret_cast<const char *>(plane + (long long)r * kRows * kP);
+    char *dst = reinterpret_cast<char *>(sm.buf);
+#pragma unroll
+    for (int q = 0; q < kCopies; ++q)
+      bulk_load(dst + q * (kChunkBytes / kCopies), src + q * (kChunkBytes / kCopies),
+                kChunkBytes / kCopies, &sm.bar);
+  }
+  for (int i = tid; i < kP; i += kPlaneThreads) sm.tw[i] = twg[i];
+  __syncthreads();
+  const bool loaded = mbar_wait_bounded(&sm.bar, 0);
+  if (!loaded) atomicExch(waitflag, 1);  // the results of this plane are then void
+
+  // y transforms of the CTA's 32 rows
+  const int t = tid & 15;
+  const int row = tid >> 4;
+  float2 v[16];
+  float2 *line = sm.buf + row * kP;
+#pragma unroll
+  for (int m = 0; m < 16; ++m) v[m] = line[t + 16 * m];
+  __syncwarp();
+  line_fft256(v, t, line, 1, sm.tw);
+
+  cluster.sync();  // every CTA is done with its rows: the buffers take column tiles
+  const int x = r * kRows + row;
+#pragma unroll
+  for (int b = 0; b < 16; ++b) {
+    // y = t + 16 b lives in CTA y / 32 = b / 2, column t + 16 (b & 1)
+    float2 *dst = cluster.map_shared_rank(sm.buf, b >> 1);
+    dst[x * kLd + t + 16 * (b & 1)] = v[b];
+  }
+  cluster.sync();  // the column tiles are complete
+
+  // x transforms of the CTA's 32 columns (16 threads each), in place
+  const int col = tid >> 4;
+  float2 *cline = sm.buf + col;
+#pragma unroll
+  for (int m = 0; m < 16; ++m) v[m] = cline[(t + 16 * m) * kLd];
+  __syncwarp();
+  line_fft256(v, t, cline, kLd, sm.tw);
+#pragma unroll
+  for (int b = 0; b < 16; ++b) cline[(t + 16 * b) * kLd] = v[b];
+  __syncthreads();
+
+  // write back: columns 32r .. 32r+31 of every x row
+  const int warp = tid >> 5, lane = tid & 31;
+  float2 *out = plane + r * kRows + lane;
+#pragma unroll 4
+  for (int xr = warp; xr < kP; xr += kPlaneThreads / 32)
+    out[(long long)xr * kP] = sm.buf[xr * kLd + lane];
+  // a CTA whose load timed out waits once more (bounded) for its copies in
+  // flight before it exits
+  if (!loaded) mbar_wait_bounded(&sm.bar, 0);
+}
+
+// update_h over plane-major sources; tile = one x row, 32 y, up to 32 kz
+constexpr int kTileY = 32, kTileK = 32;
+
+struct UhSmem {
+  float2 s[6][kTileK][kTileY + 1];
+};
+
+__global__ void __launch_bounds__(256, 4)
+    k_update_h_plane(const float2 *__restrict__ spec, const float *__restrict__ y,
+                     float *__restrict__ out, const RhsScalars *rs, Geom g, int skip_pos,
+                     double *outsc) {
+  extern __shared__ __align__(16) unsigned char uhraw[];
+  UhSmem &sm = *reinterpret_cast<UhSmem *>(uhraw);
+  const int x = blockIdx.x;
+  const int y0 = blockIdx.y * kTileY;
+  const int k0 = blockIdx.z * kTileK;
+  const int nk = min(kTileK, g.mz - k0);
+  const long long M = g.M;
+  const long long plane = (long long)g.nx * g.ny;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // the six sources: one 256-byte run along y per (array, kz)
+  for (int q = warp; q < 6 * nk; q += 8) {
+    const int a = q / nk, kl = q - a * nk;
+    const long long base = (long long)(a < 4 ? a : a + 1) * M + (long long)(k0 + kl) * plane +
+                           (long long)x * g.ny + y0;
+    sm.s[a][kl][lane] = spec[base + lane];
+  }
+  __syncthreads();
+  const TensorConsts<float> tc(rs);
+  float mx = 0.f;
+  const int kl = lane;
+  if (kl < nk) {
+    const int kz = k0 + kl;
+#pragma unroll 1
+    for (int yl = warp; yl < kTileY; yl += 8) {
+      const int j = y0 + yl;
+      const long long id = ((long long)x * g.ny + j) * g.mz + kz;
+      Mode m;
+      m.i = x;
+      m.j = j;
+      m.k = kz;
+      C2<float> n0 = mk2c<float>(0.f, 0.f), n1 = mk2c<float>(0.f, 0.f);
+      float ksq = 0.f;
+      if (id != 0) {  // the zero mode has no sources
+        const C2<float> v[6] = {sm.s[0][kl][yl], sm.s[1][kl][yl], sm.s[2][kl][yl],
+                                sm.s[3][kl][yl], sm.s[4][kl][yl], sm.s[5][kl][yl]};
+        const ModeK<float> qk = mode_k<float>(g, m);
+        ksq = qk.ksq;
+        tensor_sources<float>(m, qk, v, n0, n1);
+      }
+      HVals<float> hv;
+      tensor_load<float>(g, id, y, hv);
+      C2<float> o3, o4;
+      tensor_eom_core<float>(g, id, n0, n1, ksq, tc, hv, out, skip_pos, o3, o4);
+      mx = fmaxf(mx, fmaxf(fmaxf(fabsf(o3.x), fabsf(o3.y)), fmaxf(fabsf(o4.x), fabsf(o4.y))));
+    }
+  }
+  dh_max_store<float>(mx, outsc);
+}
+
+}  // namespace
+
+bool gw_plane_ok(const Ctx *c) {
+  return c->mixed && fused_wide_ok(c) && c->g.nx == kP && c->g.ny == kP && c->p.enable_gw &&
+         c->waitflag != nullptr;
+}
+
+int gw_plane_fft(Ctx *c, void *spec) {
+  const Geom &g = c->g;
+  const size_t smem = sizeof(PlaneSmem);
+  static_assert(sizeof(PlaneSmem) <= 113 * 1024, "two CTAs per SM");
+  IH_CUDA(c, cudaFuncSetAttribute(k_gw_plane2d, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+  const unsigned grid = (unsigned)(6LL * g.mz * kCl);
+  prof_begin(c, KK_GW_PLANE);
+  k_gw_plane2d<<<grid, kPlaneThreads, smem, c->stream>>>(
+      reinterpret_cast<float2 *>(spec), g.M, g.mz, reinterpret_cast<const float2 *>(c->tw_z),
+      c->waitflag);
+  prof_end(c, KK_GW_PLANE, 12.0 * g.M * sizeof(float2));
+  return check_launch(c, "k_gw_plane2d");
+}
+
+int update_h_plane(Ctx *c, const void *spec, const void *y, void *out, double *outsc) {
+  const Geom &g = c->g;
+  dim3 grid((unsigned)g.nx, (unsigned)(g.ny / kTileY), (unsigned)((g.mz + kTileK - 1) / kTileK));
+  const size_t smem = sizeof(UhSmem);
+  IH_CUDA(c, cudaFuncSetAttribute(k_update_h_plane, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+  prof_begin(c, KK_UPDATE_H_PLANE);
+  k_update_h_plane<<<grid, 256, smem, c->stream>>>(
+      reinterpret_cast<const float2 *>(spec), reinterpret_cast<const float *>(y),
+      reinterpret_cast<float *>(out), c->rs, g, c->skip_pos, outsc);
+  prof_end(c, KK_UPDATE_H_PLANE,
+           6.0 * g.M * sizeof(float2) + (c->skip_pos ? 6.0 : 8.0) * g.Next * sizeof(float));
+  return check_launch(c, "k_update_h_plane");
+}
+
+}  // namespace ih

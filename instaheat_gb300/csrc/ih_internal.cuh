@@ -111,6 +111,8 @@ enum KernelKind {
   KK_FILTER,            // spectral filter
   KK_LINCOMB,           // DOPRI853/RK4 stage combination
   KK_DOPRI_FINAL,       // field_new + embedded error sums
+  KK_GW_PLANE,          // y and x transforms of the tensor sources, one kz plane per cluster
+  KK_UPDATE_H_PLANE,    // update_h reading plane-major tensor sources
   KK_COUNT
 };
 const char *kernel_kind_name(int k);
@@ -222,6 +224,8 @@ struct Ctx {
   int rt_var[2] = {FV_TWOSTEP_HALF, FV_TWOSTEP_HALF};  // x, y round trips (two-step forms)
   int roundtrip = 1;  // RHS without filter/output: round trips instead of full spectra
   int tensor_fused = 0;  // update_h fused into the last x pass (autotuner's choice)
+  int gw_plane = 0;      // tensor sources plane-major: one-pass plane transforms (autotuner)
+  int *waitflag = nullptr;  // device int: a bounded device-side wait timed out
   int zwide = 1;         // the wide-row fused z pass where it applies (nz = 256, mixed)
   int gw_slab = 0;       // kz slab width of the tensor sources' y/x passes (0: whole arrays)
   int stage_fusion = 0;  // DOPRI853 stage inputs formed by the RHS of the previous stage
@@ -306,7 +310,7 @@ int fft_x_tensor(Ctx *c, const C2<T> *s03, const C2<T> *s45, T *y, T *out, doubl
 template <typename T>
 int fft_z_rhs_fused(Ctx *c, const C2<T> *d4, const T *yfl, const double *ysc,
                     T *lap, T *p, T *rho, C2<T> *s6, int gw, double *partials,
-                    int *nblocks_out, int zsrc);
+                    int *nblocks_out, int zsrc, int plane = 0);
 // The same pass on the wide-row engine (ih_zwide.cu): mixed form, nz = 256.
 bool fused_wide_ok(const Ctx *c);
 // the plain r2c z pass on the wide-row engine (same condition)
@@ -314,7 +318,11 @@ int zr2c_wide_launch(Ctx *c, const float *in, long long istride, void *out, long
                      int count);
 int fused_wide_launch(Ctx *c, const void *d4, const void *yfl, const double *ysc, void *lap,
                       void *p, void *rho, void *s6, int gw, double *partials, int *nblk_out,
-                      int zsrc);
+                      int zsrc, int plane);
+// plane-major tensor sources (ih_gwplane.cu): mixed form, 256^3, wide z pass
+bool gw_plane_ok(const Ctx *c);
+int gw_plane_fft(Ctx *c, void *spec);
+int update_h_plane(Ctx *c, const void *spec, const void *y, void *out, double *outsc);
 
 int fft_tables(Ctx *c);
 // time every engine variant of the x/y passes and the fused x pass on the

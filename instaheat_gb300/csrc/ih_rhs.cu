@@ -1074,11 +1074,13 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
     IH_TRY((fft_x_deriv4_inv<T>(c, spec + 4 * M, spec, M)));
     IH_TRY((fft_xy<T>(c, spec, M, 4, 1, +1)));
   }
-  // 3. fused inverse z + pointwise + GW products forward z
+  // 3. fused inverse z + pointwise + GW products forward z (the products
+  // plane-major where the one-pass plane transforms take them)
+  const int plane = sizeof(T) == 4 && c->gw_plane && !next && gw_plane_ok(c);
   int nblk = 0;
   if (c->g.pow2)
     IH_TRY((fft_z_rhs_fused<T>(c, spec, yfl, y.sc, lap, p, output == 1 ? rho : nullptr, spec,
-                               c->p.enable_gw, c->partials, &nblk, use_rt)));
+                               c->p.enable_gw, c->partials, &nblk, use_rt, plane)));
   else
     IH_TRY((z_pass_generic<T>(c, spec, yfl, y.sc, lap, p, output == 1 ? rho : nullptr, &nblk)));
   k_reduce_finish<<<1, 256, 0, c->stream>>>(c->partials, nblk, g, y.sc, k.sc, c->rs, c->mixed);
@@ -1090,7 +1092,10 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
     // S_ij spectra: spec[0..3] and spec[5..6]; forward y and x passes
     // (batched: per-array y-then-x ordering measured slower, no L2 reuse;
     // kz slabs of all six arrays where the autotuner chose them)
-    if (c->gw_slab > 0 && !c->tensor_fused && g.pow2) {
+    if (plane) {
+      IH_TRY(gw_plane_fft(c, spec));
+      IH_TRY(update_h_plane(c, spec, yfl, kfl, k.sc));
+    } else if (c->gw_slab > 0 && !c->tensor_fused && g.pow2) {
       IH_TRY((fft_gw_yx<T>(c, spec, c->gw_slab)));
       IH_TRY(tensor_last_pass(c, spec, yfl, kfl, k.sc, next, true));
     } else {

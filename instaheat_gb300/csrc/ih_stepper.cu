@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(256) k_dopri_final(const T *__restrict__ y, co
 // error() (dopri853.c:469-486) -> out[0]; <rho> and the NaN flag of the last
 // RHS -> out[1], out[2]
 __global__ void k_dopri_err_finish(const double *partials, int nb, const double *dtp, double ntot,
-                                   const RhsScalars *rs, double *out) {
+                                   const RhsScalars *rs, const int *waitflag, double *out) {
   const double dt = *dtp;
   double e = 0.0, e2 = 0.0;
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -514,7 +514,8 @@ __global__ void k_dopri_err_finish(const double *partials, int nb, const double 
     if (deno <= 0.0) deno = 1.0;
     out[0] = dt * err * sqrt(1.0 / (ntot * deno));
     out[1] = rs->rho_mean;
-    out[2] = (rs->nonfinite || !isfinite(out[0])) ? 1.0 : 0.0;
+    // 2: a bounded device-side wait of this try timed out; 1: NaN/Inf
+    out[2] = (waitflag && *waitflag) ? 2.0 : ((rs->nonfinite || !isfinite(out[0])) ? 1.0 : 0.0);
   }
 }
 
@@ -1065,7 +1066,7 @@ static int final_vel(Ctx *c) {
   prof_end(c, KK_DOPRI_FINAL, (double)(n + 4) * (g.Nf / 2) * sizeof(float));
   IH_TRY(check_launch(c, "k_dopri_final_vel"));
   k_dopri_err_finish<<<1, 256, 0, c->stream>>>(c->partials, (int)nb, c->dt_dev, (double)g.Ntot,
-                                               c->rs, c->diag + 4 * g.bins + 48);
+                                               c->rs, c->waitflag, c->diag + 4 * g.bins + 48);
   return check_launch(c, "k_dopri_err_finish");
 }
 
@@ -1177,7 +1178,7 @@ static int try_body(Ctx *c) {
   prof_end(c, KK_DOPRI_FINAL, 10.0 * nf * c->tsize);
   IH_TRY(check_launch(c, "k_dopri_final"));
   k_dopri_err_finish<<<1, 256, 0, c->stream>>>(c->partials, (int)nb, c->dt_dev, (double)c->g.Ntot,
-                                               c->rs, c->diag + 4 * c->g.bins + 48);
+                                               c->rs, c->waitflag, c->diag + 4 * c->g.bins + 48);
   return check_launch(c, "k_dopri_err_finish");
 }
 
@@ -1256,7 +1257,7 @@ int try_collect(Ctx *c, double *err_out, double *rho_mean_out, int *nonfinite) {
   IH_CUDA(c, cudaStreamSynchronize(c->stream));
   *err_out = c->hpin[0];
   *rho_mean_out = c->hpin[1];
-  *nonfinite = c->hpin[2] != 0.0;
+  *nonfinite = c->hpin[2] == 2.0 ? 2 : (c->hpin[2] != 0.0);
   return IH_OK;
 }
 
@@ -1346,6 +1347,10 @@ int step_accept(Ctx *c, double dt, double err, double rho_mean, int want_output,
 int try_outcome(Ctx *c, double err, double rho_mean, int nonfinite, double *dt) {
   ++c->n_tries;
   c->last_err = err;
+  if (nonfinite == 2) {
+    c->err = "a device-side wait timed out (TMA load of a tensor-source plane); results void";
+    return -IH_ERR_CUDA;
+  }
   if (nonfinite) {
     c->err = "non-finite value in the RHS reductions or the error norm";
     return -IH_ERR_NAN;

@@ -146,7 +146,12 @@ __device__ __forceinline__ float4 f4(const float2 &a, const float2 &b) {
 // ZSRC: arrays 0, 1 = d/dx Z, d/dy Z, array 3 = the laplacian (completed by
 // the y round trip), array 4 = Z (the z derivative formed here); otherwise
 // arrays 0..3 = the four full derivative spectra.
-template <bool ZSRC>
+// PLANE: the six GW source spectra are written plane-major, S[kz][x][y]
+// (row = x ny + y, element kz rows + row), for the one-pass plane transforms
+// (ih_gwplane.cu): each warp stages its four rows in its exchange buffer and
+// stores eight kz values x four consecutive y per instruction (32-byte runs;
+// the four warps of a CTA complete each 128-byte line of a kz plane).
+template <bool ZSRC, bool PLANE>
 __global__ void __launch_bounds__(32 * kWarpsW, 4) k_fft_z_rhs_wide(
     const float2 *d4, long long dstride, const float *__restrict__ yfl, const double *ysc,
     float *lap, float *pout, float *rhoout, float2 *s6, long long sstride4, float2 *s6b, int gw,
@@ -285,11 +290,28 @@ __global__ void __launch_bounds__(32 * kWarpsW, 4) k_fft_z_rhs_wide(
     zw_forward(v, t, xch, sm.twh);
     float2 xH;
     zw_r2c_post(v, t, gbase, sm.twz, xH);
-    float2 *dst = (pr < 4 ? s6 + pr * sstride4 : s6b + (pr - 4) * sstride4) + rs;
-    if (valid) {
+    if constexpr (PLANE) {
+      float2 *arr = pr < 4 ? s6 + pr * sstride4 : s6b + (pr - 4) * sstride4;
 #pragma unroll
-      for (int m = 0; m < 16; ++m) dst[t + 8 * m] = v[m];
-      if (t == 0) dst[kH] = xH;
+      for (int m = 0; m < 16; ++m) xch[t + 8 * m] = v[m];
+      if (t == 0) xch[kH] = xH;
+      __syncwarp();
+      const long long row0 = ((long long)blockIdx.x * kWarpsW + warp) * kRowsW;
+      const int gs = lane & 3;
+      const float2 *xs = sm.xch[warp][gs];
+#pragma unroll
+      for (int q = 0; q < (kH + 1 + 7) / 8; ++q) {
+        const int kz = 8 * q + (lane >> 2);
+        if (kz <= kH && row0 + gs < rows) arr[(long long)kz * rows + row0 + gs] = xs[kz];
+      }
+      __syncwarp();
+    } else {
+      float2 *dst = (pr < 4 ? s6 + pr * sstride4 : s6b + (pr - 4) * sstride4) + rs;
+      if (valid) {
+#pragma unroll
+        for (int m = 0; m < 16; ++m) dst[t + 8 * m] = v[m];
+        if (t == 0) dst[kH] = xH;
+      }
     }
   }
 }
@@ -354,9 +376,21 @@ int zr2c_wide_launch(Ctx *c, const float *in, long long istride, void *out, long
   return IH_OK;
 }
 
+template <bool ZSRC, bool PLANE>
+static void wide_launch_t(Ctx *c, unsigned nblk, size_t sm, const void *d4, long long M,
+                          const void *yfl, const double *ysc, void *lap, void *p, void *rho,
+                          float2 *s, int gw, double *partials, const Geom &g, const float2 *twh,
+                          const float2 *twz) {
+  cudaFuncSetAttribute(k_fft_z_rhs_wide<ZSRC, PLANE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sm);
+  k_fft_z_rhs_wide<ZSRC, PLANE><<<nblk, 32 * kWarpsW, sm, c->stream>>>(
+      (const float2 *)d4, M, (const float *)yfl, ysc, (float *)lap, (float *)p, (float *)rho, s, M,
+      s + 5 * M, gw, partials, g, twh, twz);
+}
+
 int fused_wide_launch(Ctx *c, const void *d4, const void *yfl, const double *ysc, void *lap,
                       void *p, void *rho, void *s6, int gw, double *partials, int *nblk_out,
-                      int zsrc) {
+                      int zsrc, int plane) {
   const Geom &g = c->g;
   const long long rows = (long long)g.nx * g.ny;
   const long long per = (long long)kRowsW * kWarpsW;
@@ -370,19 +404,14 @@ int fused_wide_launch(Ctx *c, const void *d4, const void *yfl, const double *ysc
   const float2 *twh = reinterpret_cast<const float2 *>(c->tw_h);
   const float2 *twz = reinterpret_cast<const float2 *>(c->tw_z);
   float2 *s = reinterpret_cast<float2 *>(s6);
-  if (zsrc) {
-    cudaFuncSetAttribute(k_fft_z_rhs_wide<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sm);
-    k_fft_z_rhs_wide<true><<<nblk, 32 * kWarpsW, sm, c->stream>>>(
-        (const float2 *)d4, M, (const float *)yfl, ysc, (float *)lap, (float *)p, (float *)rho, s,
-        M, s + 5 * M, gw, partials, g, twh, twz);
-  } else {
-    cudaFuncSetAttribute(k_fft_z_rhs_wide<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sm);
-    k_fft_z_rhs_wide<false><<<nblk, 32 * kWarpsW, sm, c->stream>>>(
-        (const float2 *)d4, M, (const float *)yfl, ysc, (float *)lap, (float *)p, (float *)rho, s,
-        M, s + 5 * M, gw, partials, g, twh, twz);
-  }
+  if (zsrc && plane)
+    wide_launch_t<true, true>(c, nblk, sm, d4, M, yfl, ysc, lap, p, rho, s, gw, partials, g, twh, twz);
+  else if (zsrc)
+    wide_launch_t<true, false>(c, nblk, sm, d4, M, yfl, ysc, lap, p, rho, s, gw, partials, g, twh, twz);
+  else if (plane)
+    wide_launch_t<false, true>(c, nblk, sm, d4, M, yfl, ysc, lap, p, rho, s, gw, partials, g, twh, twz);
+  else
+    wide_launch_t<false, false>(c, nblk, sm, d4, M, yfl, ysc, lap, p, rho, s, gw, partials, g, twh, twz);
   *nblk_out = (int)nblk;
   return IH_OK;
 }

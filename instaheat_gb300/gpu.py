@@ -416,9 +416,10 @@ class Context:
     def engines(self):
         """Engines of the x, y, fused x passes, the x, y round trips, the form
         of the last tensor x pass (0 separate, 1 fused), of the fused z pass
-        (1 wide rows where they apply, 0 a warp per row) and the kz slab width
-        of the tensor sources' y/x passes (0 whole arrays)."""
-        return tuple(int(self.L_.ih_fft_get_engine(self.h, p)) for p in range(8))
+        (1 wide rows where they apply, 0 a warp per row), the kz slab width
+        of the tensor sources' y/x passes (0 whole arrays) and the plane-major
+        tensor sources (1: one-pass plane transforms)."""
+        return tuple(int(self.L_.ih_fft_get_engine(self.h, p)) for p in range(9))
 
     @classmethod
     def _member(cls, handle, p: Params):

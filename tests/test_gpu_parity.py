@@ -648,3 +648,60 @@ def test_dopri853_f64_to_t10(gpu_mod, oracle_mod):
     np.testing.assert_allclose(g["gw"], d.gw, rtol=1e-8, atol=1e-14 * np.abs(d.gw).max())
     ctx.close()
     o.close()
+
+
+def test_mixed_gw_planes_match_rows(gpu_mod, oracle_mod):
+    """The tensor sources plane-major (one cluster per kz plane transforms it
+    along y and x through distributed shared memory; update_h reads the
+    planes) against the row and column passes, mixed form at 256^3: the same
+    RHS to FP32 rounding of the tensor segments (1e-5 of their magnitude),
+    the other segments identical; against the FP64 oracle's tensor RHS
+    within the mixed form's tolerance (1e-4 of the segment magnitude)."""
+    n = (256, 256, 256)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=12, amp=1e-3, hamp=1e-6)
+    ctx.set_engine(8, 0)
+    r_rows, _ = ctx.mk_rhs(f)
+    ctx.set_engine(8, 1)
+    r_pl, _ = ctx.mk_rhs(f)
+    assert ctx.engines()[8] == 1
+    N, Nx = o.N, o.Next
+    assert np.array_equal(r_rows[:4 * N], r_pl[:4 * N])
+    errs = seg_rel_err(r_pl, r_rows, N, Nx)
+    for k in ("h1", "h2", "dh1", "dh2"):
+        assert errs[k] < 1e-5, errs
+    r_ref, _ = o.rhs(f)
+    eref = seg_rel_err(r_pl, r_ref, N, Nx)
+    for k in ("dh1", "dh2"):
+        assert eref[k] < 1e-4, eref
+    ctx.close()
+    o.close()
+
+
+def test_mixed_gw_planes_dopri_steps(gpu_mod, oracle_mod):
+    """Three mixed-form DOPRI853 steps at 256^3 with the plane-major tensor
+    sources track the row/column form (same accepted steps to 1e-6, state
+    within 1e-5 of each segment's magnitude), graph-captured tries included."""
+    n = (256, 256, 256)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=13, amp=1e-3, hamp=1e-6)
+    o.close()
+    out = {}
+    for plane in (0, 1):
+        ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
+        ctx.set_engine(8, plane)
+        ctx.set_state(f)
+        ctx.dopri_init(gpu_mod.dopri_cfg(1e-8, 1e-8), 0.0, 1e-2)
+        dt, dts = 1e-2, []
+        for _ in range(3):
+            info = ctx.dopri_step(dt)
+            dts.append(info.dt_did)
+            dt = info.dt_next
+        out[plane] = (ctx.get_state(), dts)
+        ctx.close()
+    np.testing.assert_allclose(out[1][1], out[0][1], rtol=1e-6)
+    Nn = 256 ** 3
+    Nx = 2 * 256 * 256 * 129
+    errs = seg_rel_err(out[1][0], out[0][0], Nn, Nx)
+    assert max(errs.values()) < 1e-5, errs
