@@ -190,6 +190,11 @@ static int create(const ih_params *p, Ctx *c) {
   IH_CUDA(c, cudaMemsetAsync(c->diag, 0, sizeof(double) * (4 * g.bins + 128), c->stream));
   IH_TRY(dmalloc(c, (void **)&c->waitflag, sizeof(int)));
   IH_CUDA(c, cudaMemsetAsync(c->waitflag, 0, sizeof(int), c->stream));
+  if (c->mixed && p->enable_gw && g.nx == 256 && g.ny == 256 && g.nz == 256)
+  {
+    IH_TRY(dmalloc(c, &c->gwbuf, cs * (size_t)g.M * 6));
+    IH_CUDA(c, cudaMemsetAsync(c->gwbuf, 0, cs * (size_t)g.M * 6, c->stream));
+  }
   c->hpin_bytes = 4096;
   IH_CUDA(c, cudaMallocHost((void **)&c->hpin, c->hpin_bytes));
   IH_TRY(dmalloc(c, &c->stage_dev, sizeof(double) * (size_t)g.Ntot));
@@ -217,6 +222,7 @@ static void destroy(Ctx *c) {
   if (c->rs) cudaFree(c->rs);
   if (c->diag) cudaFree(c->diag);
   if (c->waitflag) cudaFree(c->waitflag);
+  if (c->gwbuf) cudaFree(c->gwbuf);
   if (c->hpin) cudaFreeHost(c->hpin);
   if (c->stage_dev) cudaFree(c->stage_dev);
   if (c->feat_dev) cudaFree(c->feat_dev);

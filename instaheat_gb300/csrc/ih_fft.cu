@@ -2316,8 +2316,8 @@ static int autotune_t(Ctx *c) {
       for (int r = 0; r <= reps && st == IH_OK; ++r) {
         if (r == 1) cudaEventRecord(e0, c->stream);
         if (v == 1) {
-          st = gw_plane_fft(c, sp);
-          if (st == IH_OK) st = update_h_plane(c, sp, c->y.fl, c->ytmp.fl, c->ytmp.sc);
+          st = gw_plane_fft(c, c->gwbuf);
+          if (st == IH_OK) st = update_h_plane(c, c->gwbuf, c->y.fl, c->ytmp.fl, c->ytmp.sc);
           if (st != IH_OK) {  // e.g. no room for a cluster of 8: keep the row passes
             snprintf(line, sizeof line, "gw planes unavailable (%s); ", c->err.c_str());
             rep += line;

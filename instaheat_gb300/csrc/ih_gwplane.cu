@@ -3,7 +3,8 @@
 // (mixed form, 256^3).
 //
 // The six S_ij spectra are written by the fused z pass plane-major,
-// S[a][kz][x][y] (each kz plane a contiguous 256 x 256 complex block), so
+// S[a][kz][x][y] (each kz plane a contiguous 256 x 256 complex block; the
+// six arrays consecutive in their own buffer, Ctx::gwbuf), so
 // that one plane's forward y and x transforms can run in one read and one
 // write of the plane instead of a y pass and an x pass over whole arrays
 // (half the HBM traffic of the row/column engines on these arrays).
@@ -128,8 +129,7 @@ __device__ __forceinline__ void line_fft256(float2 (&v)[16], int t, float2 *line
 }
 
 // One kz plane of one of the six S_ij spectra per cluster: forward y then x
-// transforms, in place.  spec: the complex spectra of the RHS (slots 0..3
-// and 5, 6 hold the sources), M complex each.
+// transforms, in place.  src: the six plane-major spectra, M complex each.
 __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kPlaneThreads, 2)
     k_gw_plane2d(float2 *spec, long long M, int mz, const float2 *__restrict__ twg, int *waitflag) {
   extern __shared__ __align__(128) unsigned char smraw[];
@@ -139,7 +139,7 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kPlaneThreads, 2)
   const int tid = threadIdx.x;
   const long long p = blockIdx.x / kCl;          // plane: array a, kz
   const int a = (int)(p / mz), kz = (int)(p % mz);
-  float2 *plane = spec + (long long)(a < 4 ? a : a + 1) * M + (long long)kz * kP * kP;
+  float2 *plane = spec + (long long)a * M + (long long)kz * kP * kP;
 
   if (tid == 0) {
     mbar_init(&sm.bar, 1);
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256, 4)
   // the six sources: one 256-byte run along y per (array, kz)
   for (int q = warp; q < 6 * nk; q += 8) {
     const int a = q / nk, kl = q - a * nk;
-    const long long base = (long long)(a < 4 ? a : a + 1) * M + (long long)(k0 + kl) * plane +
+    const long long base = (long long)a * M + (long long)(k0 + kl) * plane +
                            (long long)x * g.ny + y0;
     sm.s[a][kl][lane] = spec[base + lane];
   }
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(256, 4)
 
 bool gw_plane_ok(const Ctx *c) {
   return c->mixed && fused_wide_ok(c) && c->g.nx == kP && c->g.ny == kP && c->p.enable_gw &&
-         c->waitflag != nullptr;
+         c->waitflag != nullptr && c->gwbuf != nullptr;
 }
 
 int gw_plane_fft(Ctx *c, void *spec) {

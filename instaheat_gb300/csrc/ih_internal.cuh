@@ -226,6 +226,7 @@ struct Ctx {
   int tensor_fused = 0;  // update_h fused into the last x pass (autotuner's choice)
   int gw_plane = 0;      // tensor sources plane-major: one-pass plane transforms (autotuner)
   int *waitflag = nullptr;  // device int: a bounded device-side wait timed out
+  void *gwbuf = nullptr;    // plane-major tensor sources: 6 spectra of M complex (T)
   int zwide = 1;         // the wide-row fused z pass where it applies (nz = 256, mixed)
   int gw_slab = 0;       // kz slab width of the tensor sources' y/x passes (0: whole arrays)
   int stage_fusion = 0;  // DOPRI853 stage inputs formed by the RHS of the previous stage
@@ -319,7 +320,10 @@ int zr2c_wide_launch(Ctx *c, const float *in, long long istride, void *out, long
 int fused_wide_launch(Ctx *c, const void *d4, const void *yfl, const double *ysc, void *lap,
                       void *p, void *rho, void *s6, int gw, double *partials, int *nblk_out,
                       int zsrc, int plane);
-// plane-major tensor sources (ih_gwplane.cu): mixed form, 256^3, wide z pass
+// plane-major tensor sources (ih_gwplane.cu): mixed form, 256^3, wide z pass;
+// the six sources live in Ctx::gwbuf (a plane-major write would otherwise
+// land in rows of the derivative spectra that other CTAs of the z pass have
+// not read yet)
 bool gw_plane_ok(const Ctx *c);
 int gw_plane_fft(Ctx *c, void *spec);
 int update_h_plane(Ctx *c, const void *spec, const void *y, void *out, double *outsc);

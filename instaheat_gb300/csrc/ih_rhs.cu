@@ -1079,8 +1079,9 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
   const int plane = sizeof(T) == 4 && c->gw_plane && !next && gw_plane_ok(c);
   int nblk = 0;
   if (c->g.pow2)
-    IH_TRY((fft_z_rhs_fused<T>(c, spec, yfl, y.sc, lap, p, output == 1 ? rho : nullptr, spec,
-                               c->p.enable_gw, c->partials, &nblk, use_rt, plane)));
+    IH_TRY((fft_z_rhs_fused<T>(c, spec, yfl, y.sc, lap, p, output == 1 ? rho : nullptr,
+                               plane ? (C2<T> *)c->gwbuf : spec, c->p.enable_gw, c->partials,
+                               &nblk, use_rt, plane)));
   else
     IH_TRY((z_pass_generic<T>(c, spec, yfl, y.sc, lap, p, output == 1 ? rho : nullptr, &nblk)));
   k_reduce_finish<<<1, 256, 0, c->stream>>>(c->partials, nblk, g, y.sc, k.sc, c->rs, c->mixed);
@@ -1093,8 +1094,8 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
     // (batched: per-array y-then-x ordering measured slower, no L2 reuse;
     // kz slabs of all six arrays where the autotuner chose them)
     if (plane) {
-      IH_TRY(gw_plane_fft(c, spec));
-      IH_TRY(update_h_plane(c, spec, yfl, kfl, k.sc));
+      IH_TRY(gw_plane_fft(c, c->gwbuf));
+      IH_TRY(update_h_plane(c, c->gwbuf, yfl, kfl, k.sc));
     } else if (c->gw_slab > 0 && !c->tensor_fused && g.pow2) {
       IH_TRY((fft_gw_yx<T>(c, spec, c->gw_slab)));
       IH_TRY(tensor_last_pass(c, spec, yfl, kfl, k.sc, next, true));

@@ -383,9 +383,11 @@ static void wide_launch_t(Ctx *c, unsigned nblk, size_t sm, const void *d4, long
                           const float2 *twz) {
   cudaFuncSetAttribute(k_fft_z_rhs_wide<ZSRC, PLANE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sm);
+  // row layout: the sources in spectra 0..3, 5, 6 of the RHS block; plane
+  // layout: six consecutive spectra of their own buffer
   k_fft_z_rhs_wide<ZSRC, PLANE><<<nblk, 32 * kWarpsW, sm, c->stream>>>(
       (const float2 *)d4, M, (const float *)yfl, ysc, (float *)lap, (float *)p, (float *)rho, s, M,
-      s + 5 * M, gw, partials, g, twh, twz);
+      s + (PLANE ? 4 : 5) * M, gw, partials, g, twh, twz);
 }
 
 int fused_wide_launch(Ctx *c, const void *d4, const void *yfl, const double *ysc, void *lap,
