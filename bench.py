@@ -245,7 +245,8 @@ def bench_form(gpu, precision, device, seed, steps, warmup, profile=False, clock
                           | {"tensor_x": ("fused" if ctx.engines()[5] else "separate"),
                              "z_fused": ("wide rows" if ctx.engines()[6] else "warp rows"),
                              "gw_yx_slab": ctx.engines()[7],
-                             "gw_planes": bool(ctx.engines()[8])},
+                             "gw_planes": ("persistent planes", "planes", "rows")[
+                                 2 - ctx.engines()[8]]},
            "fft_autotune": ctx.autotune_report}
     return ctx, res
 

@@ -197,10 +197,12 @@ const char *ih_autotune_report(const ih_context *c);
  * (0 = whole arrays, the default; a multiple of 8 up to 64 = y then x pass on
  * one slab of all six at a time, so the slab stays in L2 between the two; it
  * applies with pass 5 = 0), 8 = the tensor sources plane-major (1: the fused
- * z pass writes each source as 129 contiguous 256 x 256 kz planes, one
- * cluster of 8 CTAs transforms a plane along y and x in one pass through
- * distributed shared memory, and update_h reads the planes; mixed form at
- * 256^3 only, IH_ERR_ARG elsewhere; 0: the row and column passes);
+ * z pass writes each source as 129 contiguous 256 x 256 kz planes into a
+ * buffer of their own, one cluster of 8 CTAs transforms a plane along y and x
+ * in one pass through distributed shared memory, and update_h reads the
+ * planes; 2: the same with persistent clusters that load the next plane
+ * while they transform the current one; mixed form at 256^3 only,
+ * IH_ERR_ARG elsewhere; 0: the row and column passes);
  * engine IH_FFT_STOCKHAM, IH_FFT_TWOSTEP (register two-step,
  * 128-byte tiles), IH_FFT_TWOSTEP_HALF (64-byte tiles), IH_FFT_PIPELINED
  * (register two-step in persistent CTAs that copy the next tile in with

@@ -512,8 +512,8 @@ const char *ih_autotune_report(const ih_context *h) {
 int ih_fft_set_engine(ih_context *h, int pass, int engine) {
   CTX_CHECK(h);
   if (pass == 8) {  // plane-major tensor sources with the one-pass plane transforms
-    if (engine < 0 || engine > 1) return IH_ERR_ARG;
-    if (engine == 1 && !gw_plane_ok(&h->c)) {
+    if (engine < 0 || engine > 2) return IH_ERR_ARG;
+    if (engine > 0 && !gw_plane_ok(&h->c)) {
       h->c.err = "the plane transforms apply to the mixed form at 256^3 with GW on";
       return IH_ERR_ARG;
     }

@@ -2310,13 +2310,13 @@ static int autotune_t(Ctx *c) {
   // transforms on plane-major sources
   c->gw_plane = 0;
   if (st == IH_OK && sizeof(T) == 4 && gw_plane_ok(c)) {
-    float tail[2] = {0.f, 0.f};
+    float tail[3] = {0.f, 0.f, 0.f};
     bool planes_usable = true;
-    for (int v = 0; v < 2 && st == IH_OK; ++v) {
+    for (int v = 0; v < 3 && st == IH_OK; ++v) {
       for (int r = 0; r <= reps && st == IH_OK; ++r) {
         if (r == 1) cudaEventRecord(e0, c->stream);
-        if (v == 1) {
-          st = gw_plane_fft(c, c->gwbuf);
+        if (v >= 1) {
+          st = gw_plane_fft(c, c->gwbuf, v);
           if (st == IH_OK) st = update_h_plane(c, c->gwbuf, c->y.fl, c->ytmp.fl, c->ytmp.sc);
           if (st != IH_OK) {  // e.g. no room for a cluster of 8: keep the row passes
             snprintf(line, sizeof line, "gw planes unavailable (%s); ", c->err.c_str());
@@ -2348,9 +2348,12 @@ static int autotune_t(Ctx *c) {
       tail[v] /= reps;
     }
     if (st == IH_OK && planes_usable) {
-      c->gw_plane = tail[1] < tail[0];
-      snprintf(line, sizeof line, "gw tail rows %.1f us, planes %.1f us; ", 1e3 * tail[0],
-               1e3 * tail[1]);
+      c->gw_plane = 0;
+      for (int v = 1; v < 3; ++v)
+        if (tail[v] < tail[c->gw_plane]) c->gw_plane = v;
+      snprintf(line, sizeof line,
+               "gw tail rows %.1f us, planes %.1f us, persistent planes %.1f us; ",
+               1e3 * tail[0], 1e3 * tail[1], 1e3 * tail[2]);
       rep += line;
     }
   }

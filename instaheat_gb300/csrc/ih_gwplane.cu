@@ -198,6 +198,91 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kPlaneThreads, 2)
   if (!loaded) mbar_wait_bounded(&sm.bar, 0);
 }
 
+// Persistent form: each cluster walks planes p = cluster, cluster + clusters,
+// ... with two buffers per CTA; while plane i is transformed, the TMA load of
+// plane i + 1 is already in flight (issued when plane i - 1's buffer was
+// released), so the memory pipe does not idle during the transforms.  One
+// CTA per SM (two 67.6 KB buffers); the grid holds exactly the clusters that
+// can be resident.  Same arithmetic as k_gw_plane2d.
+struct PlaneSmem2 {
+  float2 buf[2][kP * kLd];
+  float2 tw[kP];
+  unsigned long long bar[2];
+};
+
+__device__ __forceinline__ void load_chunk(float2 *spec, long long M, int mz, long long p, int r,
+                                           float2 *dst, unsigned long long *bar) {
+  const int a = (int)(p / mz), kz = (int)(p % mz);
+  const float2 *plane = spec + (long long)a * M + (long long)kz * kP * kP;
+  const char *src = reinterpret_cast<const char *>(plane + (long long)r * kRows * kP);
+  mbar_expect_tx(bar, kChunkBytes);
+#pragma unroll
+  for (int q = 0; q < kCopies; ++q)
+    bulk_load(reinterpret_cast<char *>(dst) + q * (kChunkBytes / kCopies),
+              src + q * (kChunkBytes / kCopies), kChunkBytes / kCopies, bar);
+}
+
+__global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kPlaneThreads, 1)
+    k_gw_plane2p(float2 *spec, long long M, int mz, long long nplanes,
+                 const float2 *__restrict__ twg, int *waitflag) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  PlaneSmem2 &sm = *reinterpret_cast<PlaneSmem2 *>(smraw);
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const int tid = threadIdx.x;
+  const long long cid = blockIdx.x / kCl, ncl = gridDim.x / kCl;
+  if (tid == 0) {
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
+    if (cid < nplanes) load_chunk(spec, M, mz, cid, r, sm.buf[0], &sm.bar[0]);
+    if (cid + ncl < nplanes) load_chunk(spec, M, mz, cid + ncl, r, sm.buf[1], &sm.bar[1]);
+  }
+  for (int i = tid; i < kP; i += kPlaneThreads) sm.tw[i] = twg[i];
+  __syncthreads();
+  const int t = tid & 15, row = tid >> 4, col = tid >> 4;
+  const int warp = tid >> 5, lane = tid & 31;
+  int it = 0;
+  for (long long p = cid; p < nplanes; p += ncl, ++it) {
+    const int cur = it & 1;
+    float2 *buf = sm.buf[cur];
+    if (!mbar_wait_bounded(&sm.bar[cur], (unsigned)((it >> 1) & 1))) atomicExch(waitflag, 1);
+    // y transforms of the CTA's 32 rows
+    float2 v[16];
+    float2 *line = buf + row * kP;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = line[t + 16 * m];
+    __syncwarp();
+    line_fft256(v, t, line, 1, sm.tw);
+    cluster.sync();
+    const int x = r * kRows + row;
+#pragma unroll
+    for (int b = 0; b < 16; ++b) {
+      float2 *dst = cluster.map_shared_rank(buf, b >> 1);
+      dst[x * kLd + t + 16 * (b & 1)] = v[b];
+    }
+    cluster.sync();
+    // x transforms of the CTA's 32 columns
+    float2 *cline = buf + col;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = cline[(t + 16 * m) * kLd];
+    __syncwarp();
+    line_fft256(v, t, cline, kLd, sm.tw);
+#pragma unroll
+    for (int b = 0; b < 16; ++b) cline[(t + 16 * b) * kLd] = v[b];
+    __syncthreads();
+    const int a = (int)(p / mz), kz = (int)(p % mz);
+    float2 *out = spec + (long long)a * M + (long long)kz * kP * kP + r * kRows + lane;
+#pragma unroll 4
+    for (int xr = warp; xr < kP; xr += kPlaneThreads / 32)
+      out[(long long)xr * kP] = buf[xr * kLd + lane];
+    __syncthreads();  // every read of buf is done: it takes the plane after next
+    if (tid == 0 && p + 2 * ncl < nplanes) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      load_chunk(spec, M, mz, p + 2 * ncl, r, buf, &sm.bar[cur]);
+    }
+  }
+}
+
 // update_h over plane-major sources; tile = one x row, 32 y, up to 32 kz
 constexpr int kTileY = 32, kTileK = 32;
 
@@ -205,7 +290,7 @@ struct UhSmem {
   float2 s[6][kTileK][kTileY + 1];
 };
 
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, 3)
     k_update_h_plane(const float2 *__restrict__ spec, const float *__restrict__ y,
                      float *__restrict__ out, const RhsScalars *rs, Geom g, int skip_pos,
                      double *outsc) {
@@ -231,8 +316,15 @@ __global__ void __launch_bounds__(256, 4)
   const int kl = lane;
   if (kl < nk) {
     const int kz = k0 + kl;
-#pragma unroll 1
-    for (int yl = warp; yl < kTileY; yl += 8) {
+    // the state's tensor entries of the thread's four modes, loaded before
+    // any arithmetic so that all sixteen loads are in flight together
+    HVals<float> hq[kTileY / 8];
+#pragma unroll
+    for (int q = 0; q < kTileY / 8; ++q)
+      tensor_load<float>(g, ((long long)x * g.ny + y0 + warp + 8 * q) * g.mz + kz, y, hq[q]);
+#pragma unroll
+    for (int q = 0; q < kTileY / 8; ++q) {
+      const int yl = warp + 8 * q;
       const int j = y0 + yl;
       const long long id = ((long long)x * g.ny + j) * g.mz + kz;
       Mode m;
@@ -248,10 +340,8 @@ __global__ void __launch_bounds__(256, 4)
         ksq = qk.ksq;
         tensor_sources<float>(m, qk, v, n0, n1);
       }
-      HVals<float> hv;
-      tensor_load<float>(g, id, y, hv);
       C2<float> o3, o4;
-      tensor_eom_core<float>(g, id, n0, n1, ksq, tc, hv, out, skip_pos, o3, o4);
+      tensor_eom_core<float>(g, id, n0, n1, ksq, tc, hq[q], out, skip_pos, o3, o4);
       mx = fmaxf(mx, fmaxf(fmaxf(fabsf(o3.x), fabsf(o3.y)), fmaxf(fabsf(o4.x), fabsf(o4.y))));
     }
   }
@@ -265,19 +355,46 @@ bool gw_plane_ok(const Ctx *c) {
          c->waitflag != nullptr && c->gwbuf != nullptr;
 }
 
-int gw_plane_fft(Ctx *c, void *spec) {
+// form 1: one cluster per plane; form 2: persistent clusters with the next
+// plane's load in flight
+int gw_plane_fft(Ctx *c, void *spec, int form) {
   const Geom &g = c->g;
-  const size_t smem = sizeof(PlaneSmem);
-  static_assert(sizeof(PlaneSmem) <= 113 * 1024, "two CTAs per SM");
-  IH_CUDA(c, cudaFuncSetAttribute(k_gw_plane2d, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-  const unsigned grid = (unsigned)(6LL * g.mz * kCl);
+  const long long nplanes = 6LL * g.mz;
   prof_begin(c, KK_GW_PLANE);
-  k_gw_plane2d<<<grid, kPlaneThreads, smem, c->stream>>>(
-      reinterpret_cast<float2 *>(spec), g.M, g.mz, reinterpret_cast<const float2 *>(c->tw_z),
-      c->waitflag);
+  if (form == 2) {
+    const size_t smem = sizeof(PlaneSmem2);
+    IH_CUDA(c, cudaFuncSetAttribute(k_gw_plane2p, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+    if (c->gw_clusters <= 0) {
+      // the clusters that can be resident at once: the persistent grid
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(kCl * 64, 1, 1);
+      cfg.blockDim = dim3(kPlaneThreads, 1, 1);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = c->stream;
+      int ncl = 0;
+      IH_CUDA(c, cudaOccupancyMaxActiveClusters(&ncl, (const void *)k_gw_plane2p, &cfg));
+      if (ncl < 1) {
+        c->err = "no cluster of 8 CTAs fits the device";
+        return IH_ERR_CUDA;
+      }
+      c->gw_clusters = ncl;
+    }
+    const long long ncl = c->gw_clusters < nplanes ? c->gw_clusters : nplanes;
+    k_gw_plane2p<<<(unsigned)(ncl * kCl), kPlaneThreads, smem, c->stream>>>(
+        reinterpret_cast<float2 *>(spec), g.M, g.mz, nplanes,
+        reinterpret_cast<const float2 *>(c->tw_z), c->waitflag);
+  } else {
+    const size_t smem = sizeof(PlaneSmem);
+    static_assert(sizeof(PlaneSmem) <= 113 * 1024, "two CTAs per SM");
+    IH_CUDA(c, cudaFuncSetAttribute(k_gw_plane2d, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+    k_gw_plane2d<<<(unsigned)(nplanes * kCl), kPlaneThreads, smem, c->stream>>>(
+        reinterpret_cast<float2 *>(spec), g.M, g.mz, reinterpret_cast<const float2 *>(c->tw_z),
+        c->waitflag);
+  }
   prof_end(c, KK_GW_PLANE, 12.0 * g.M * sizeof(float2));
-  return check_launch(c, "k_gw_plane2d");
+  return check_launch(c, form == 2 ? "k_gw_plane2p" : "k_gw_plane2d");
 }
 
 int update_h_plane(Ctx *c, const void *spec, const void *y, void *out, double *outsc) {

@@ -224,7 +224,8 @@ struct Ctx {
   int rt_var[2] = {FV_TWOSTEP_HALF, FV_TWOSTEP_HALF};  // x, y round trips (two-step forms)
   int roundtrip = 1;  // RHS without filter/output: round trips instead of full spectra
   int tensor_fused = 0;  // update_h fused into the last x pass (autotuner's choice)
-  int gw_plane = 0;      // tensor sources plane-major: one-pass plane transforms (autotuner)
+  int gw_plane = 0;      // tensor sources plane-major: 1 one cluster per plane, 2 persistent
+  int gw_clusters = 0;   // resident clusters of the persistent plane transforms
   int *waitflag = nullptr;  // device int: a bounded device-side wait timed out
   void *gwbuf = nullptr;    // plane-major tensor sources: 6 spectra of M complex (T)
   int zwide = 1;         // the wide-row fused z pass where it applies (nz = 256, mixed)
@@ -325,7 +326,7 @@ int fused_wide_launch(Ctx *c, const void *d4, const void *yfl, const double *ysc
 // land in rows of the derivative spectra that other CTAs of the z pass have
 // not read yet)
 bool gw_plane_ok(const Ctx *c);
-int gw_plane_fft(Ctx *c, void *spec);
+int gw_plane_fft(Ctx *c, void *spec, int form);
 int update_h_plane(Ctx *c, const void *spec, const void *y, void *out, double *outsc);
 
 int fft_tables(Ctx *c);

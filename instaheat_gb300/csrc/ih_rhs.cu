@@ -1094,7 +1094,7 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
     // (batched: per-array y-then-x ordering measured slower, no L2 reuse;
     // kz slabs of all six arrays where the autotuner chose them)
     if (plane) {
-      IH_TRY(gw_plane_fft(c, c->gwbuf));
+      IH_TRY(gw_plane_fft(c, c->gwbuf, c->gw_plane));
       IH_TRY(update_h_plane(c, c->gwbuf, yfl, kfl, k.sc));
     } else if (c->gw_slab > 0 && !c->tensor_fused && g.pow2) {
       IH_TRY((fft_gw_yx<T>(c, spec, c->gw_slab)));

@@ -418,7 +418,7 @@ class Context:
         of the last tensor x pass (0 separate, 1 fused), of the fused z pass
         (1 wide rows where they apply, 0 a warp per row), the kz slab width
         of the tensor sources' y/x passes (0 whole arrays) and the plane-major
-        tensor sources (1: one-pass plane transforms)."""
+        tensor sources (0 rows, 1 one cluster per plane, 2 persistent clusters)."""
         return tuple(int(self.L_.ih_fft_get_engine(self.h, p)) for p in range(9))
 
     @classmethod

@@ -650,22 +650,25 @@ def test_dopri853_f64_to_t10(gpu_mod, oracle_mod):
     o.close()
 
 
-def test_mixed_gw_planes_match_rows(gpu_mod, oracle_mod):
+@pytest.mark.parametrize("form", [1, 2])
+def test_mixed_gw_planes_match_rows(gpu_mod, oracle_mod, form):
     """The tensor sources plane-major (one cluster per kz plane transforms it
     along y and x through distributed shared memory; update_h reads the
     planes) against the row and column passes, mixed form at 256^3: the same
     RHS to FP32 rounding of the tensor segments (1e-5 of their magnitude),
     the other segments identical; against the FP64 oracle's tensor RHS
-    within the mixed form's tolerance (1e-4 of the segment magnitude)."""
+    within the mixed form's tolerance (1e-4 of the segment magnitude).
+    Form 1: one cluster per plane; form 2: persistent clusters prefetching
+    the next plane."""
     n = (256, 256, 256)
     ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
     o = oracle_mod.Oracle(n=n)
     f = make_state(o, seed=12, amp=1e-3, hamp=1e-6)
     ctx.set_engine(8, 0)
     r_rows, _ = ctx.mk_rhs(f)
-    ctx.set_engine(8, 1)
+    ctx.set_engine(8, form)
     r_pl, _ = ctx.mk_rhs(f)
-    assert ctx.engines()[8] == 1
+    assert ctx.engines()[8] == form
     N, Nx = o.N, o.Next
     assert np.array_equal(r_rows[:4 * N], r_pl[:4 * N])
     errs = seg_rel_err(r_pl, r_rows, N, Nx)
@@ -679,7 +682,8 @@ def test_mixed_gw_planes_match_rows(gpu_mod, oracle_mod):
     o.close()
 
 
-def test_mixed_gw_planes_dopri_steps(gpu_mod, oracle_mod):
+@pytest.mark.parametrize("form", [1, 2])
+def test_mixed_gw_planes_dopri_steps(gpu_mod, oracle_mod, form):
     """Three mixed-form DOPRI853 steps at 256^3 with the plane-major tensor
     sources track the row/column form (same accepted steps to 1e-6, state
     within 1e-5 of each segment's magnitude), graph-captured tries included."""
@@ -688,7 +692,7 @@ def test_mixed_gw_planes_dopri_steps(gpu_mod, oracle_mod):
     f = make_state(o, seed=13, amp=1e-3, hamp=1e-6)
     o.close()
     out = {}
-    for plane in (0, 1):
+    for plane in (0, form):
         ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
         ctx.set_engine(8, plane)
         ctx.set_state(f)
@@ -700,8 +704,8 @@ def test_mixed_gw_planes_dopri_steps(gpu_mod, oracle_mod):
             dt = info.dt_next
         out[plane] = (ctx.get_state(), dts)
         ctx.close()
-    np.testing.assert_allclose(out[1][1], out[0][1], rtol=1e-6)
+    np.testing.assert_allclose(out[form][1], out[0][1], rtol=1e-6)
     Nn = 256 ** 3
     Nx = 2 * 256 * 256 * 129
-    errs = seg_rel_err(out[1][0], out[0][0], Nn, Nx)
+    errs = seg_rel_err(out[form][0], out[0][0], Nn, Nx)
     assert max(errs.values()) < 1e-5, errs
