@@ -445,6 +445,11 @@ int ih_host_free(void *p);
  * CUDA-event-timed launches after one warm-up.  The ALU roofline of the
  * plain FP64 form. */
 int ih_fp64_fma_peak(int device, int iters, int reps, double *tflops);
+/* The tensor sources' plane transforms (ih_fft_set_engine pass 8: form 1 one
+ * cluster per plane, 2 persistent clusters) alone on a zeroed buffer of six
+ * 256 x 256 x mz complex FP32 spectra (mz = 129 at 256^3: 405 MB), `reps`
+ * CUDA-event-timed launches after one warm-up: milliseconds per launch. */
+int ih_gw_plane_probe(int device, int form, int mz, int reps, double *ms_per_launch);
 
 #ifdef __cplusplus
 }

@@ -413,3 +413,71 @@ int update_h_plane(Ctx *c, const void *spec, const void *y, void *out, double *o
 }
 
 }  // namespace ih
+
+// ---------------------------------------------------------------------------
+// measurement: the plane transforms alone on a buffer of their own (six
+// spectra of 256 x 256 x mz complex FP32, mz = 129 for 256^3: 405 MB, larger
+// than L2), for CUDA-event timing and small-case profiling.  No reference
+// counterpart.
+extern "C" int ih_gw_plane_probe(int device, int form, int mz, int reps, double *ms_per_launch) {
+  using namespace ih;
+  if (!ms_per_launch || reps < 1 || mz < 1 || (form != 1 && form != 2)) return IH_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return IH_ERR_CUDA;
+  const long long M = (long long)kP * kP * mz, nplanes = 6LL * mz;
+  float2 *buf = nullptr, *tw = nullptr;
+  int *flag = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int st = IH_ERR_CUDA;
+  float ms = 0.f;
+  int ncl = 0;
+  float2 htw[kP];
+  for (int k = 0; k < kP; ++k) {
+    const double ang = 6.283185307179586476925286766559 * k / kP;
+    htw[k] = make_float2((float)cos(ang), (float)-sin(ang));
+  }
+  if (cudaMalloc(&buf, sizeof(float2) * 6 * M) != cudaSuccess) return IH_ERR_ALLOC;
+  if (cudaMalloc(&tw, sizeof htw) != cudaSuccess || cudaMalloc(&flag, sizeof(int)) != cudaSuccess)
+    goto done;
+  if (cudaMemset(buf, 0, sizeof(float2) * 6 * M) != cudaSuccess ||
+      cudaMemset(flag, 0, sizeof(int)) != cudaSuccess ||
+      cudaMemcpy(tw, htw, sizeof htw, cudaMemcpyHostToDevice) != cudaSuccess)
+    goto done;
+  if (cudaFuncSetAttribute(k_gw_plane2d, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sizeof(PlaneSmem)) != cudaSuccess ||
+      cudaFuncSetAttribute(k_gw_plane2p, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sizeof(PlaneSmem2)) != cudaSuccess)
+    goto done;
+  if (form == 2) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kCl * 64, 1, 1);
+    cfg.blockDim = dim3(kPlaneThreads, 1, 1);
+    cfg.dynamicSmemBytes = sizeof(PlaneSmem2);
+    if (cudaOccupancyMaxActiveClusters(&ncl, (const void *)k_gw_plane2p, &cfg) != cudaSuccess ||
+        ncl < 1)
+      goto done;
+    if (ncl > nplanes) ncl = (int)nplanes;
+  }
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) goto done;
+  for (int r = 0; r <= reps; ++r) {  // r = 0: warm-up
+    if (r == 1) cudaEventRecord(e0);
+    if (form == 2)
+      k_gw_plane2p<<<(unsigned)(ncl * kCl), kPlaneThreads, sizeof(PlaneSmem2)>>>(buf, M, mz, nplanes,
+                                                                                tw, flag);
+    else
+      k_gw_plane2d<<<(unsigned)(nplanes * kCl), kPlaneThreads, sizeof(PlaneSmem)>>>(buf, M, mz, tw,
+                                                                                   flag);
+    if (cudaGetLastError() != cudaSuccess) goto done;
+  }
+  cudaEventRecord(e1);
+  if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+    goto done;
+  *ms_per_launch = ms / reps;
+  st = IH_OK;
+done:
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(buf);
+  cudaFree(tw);
+  cudaFree(flag);
+  return st;
+}

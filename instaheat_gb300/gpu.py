@@ -173,8 +173,19 @@ def load(build_if_missing: bool = True):
     L.ih_ensemble_run.argtypes = [vp, C.c_double, C.c_long, C.POINTER(C.c_long),
                                   C.POINTER(C.c_long)]
     L.ih_fp64_fma_peak.argtypes = [C.c_int, C.c_int, C.c_int, _dp]
+    L.ih_gw_plane_probe.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp]
     _lib = L
     return L
+
+
+def gw_plane_probe(form, mz=129, reps=20, device=0) -> float:
+    """Milliseconds per launch of the tensor sources' plane transforms alone
+    (ih_gw_plane_probe; form 1 one cluster per plane, 2 persistent)."""
+    v = C.c_double()
+    st = load().ih_gw_plane_probe(device, form, mz, reps, C.byref(v))
+    if st != 0:
+        raise IHError(st, "ih_gw_plane_probe")
+    return v.value
 
 
 def fp64_fma_peak(device=0, iters=8192, reps=5) -> float:
