@@ -51,7 +51,7 @@ enum { IH_PREC_F64 = 0, IH_PREC_MIXED = 1 };
 typedef struct {
     int nx, ny, nz;        /* GRIDPOINTS_X/Y/Z: 2^a 3^b (a >= 1; powers of two take
                               the tuned engines, a factor 3 the mixed-radix route),
-                              nx >= ny >= nz >= 8, nx <= 256 (FP64) or 512 (mixed) */
+                              nx >= ny >= nz >= 8, nx <= 512 */
     double lx, ly, lz;     /* SPATIAL_UPPER_BOUND_* - SPATIAL_LOWER_BOUND_* */
     double mass;           /* MASS (V = m^2 phi^2 / 2) */
     int enable_gw;         /* ENABLE_GW */

@@ -76,10 +76,8 @@ static int validate(const ih_params *p, std::string *why) {
     *why = "the 3D GPU path needs nz >= 8";
     return IH_ERR_ARG;
   }
-  const int nmax = p->precision == IH_PREC_MIXED ? 512 : 256;
-  if (p->nx > nmax || p->nz > nmax) {
-    *why = "grid too large for the FFT tiles (every axis <= 256 in FP64, <= 512 in the mixed "
-           "form)";
+  if (p->nx > 512 || p->nz > 512) {
+    *why = "grid too large for the FFT tiles (every axis <= 512)";
     return IH_ERR_ARG;
   }
   if (!(p->lx > 0 && p->ly > 0 && p->lz > 0)) {

@@ -1620,7 +1620,9 @@ static int dispatch_len(int L, F &&f, bool allow512) {
   return IH_ERR_ARG;
 }
 
-template <typename T> constexpr bool allow512() { return sizeof(T) == 4; }
+// 512-point passes in both precisions (FP64 ones spill in some forms; the
+// autotuner times them like the rest)
+template <typename T> constexpr bool allow512() { return true; }
 
 // threads of a Stockham tile: B*L/(4K) radix-4 butterflies, at most K each
 static int threads_st(int L, int B) {

@@ -92,7 +92,7 @@ def load(path=DEFAULT_MODEL, device=0):
 
 
 # the largest grid the FP64 form runs (its FFT tiles)
-F64_MAX_N = 256
+F64_MAX_N = 512
 
 
 def evaluate(n, seed, t_end, model=DEFAULT_MODEL, rtol=1e-8, device=0, amp=1e-3):

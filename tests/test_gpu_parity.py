@@ -709,3 +709,31 @@ def test_mixed_gw_planes_dopri_steps(gpu_mod, oracle_mod, form):
     Nx = 2 * 256 * 256 * 129
     errs = seg_rel_err(out[form][0], out[0][0], Nn, Nx)
     assert max(errs.values()) < 1e-5, errs
+
+
+def test_rhs_f64_parity_512(gpu_mod, oracle_mod):
+    """Plain FP64 mk_rhs at 512^3 (the largest grid; the FP64 arbiter of the
+    512^3 runs), filter and output on, within 1e-11 of each segment.  The
+    CPU oracle and the host copies need about 80 GB of host memory: skipped
+    on a host with less than 200 GB available."""
+    try:
+        avail = int([ln for ln in open("/proc/meminfo") if ln.startswith("MemAvailable")][0]
+                    .split()[1]) * 1024
+    except (OSError, IndexError, ValueError):
+        avail = 0
+    if avail < 200e9:
+        pytest.skip(f"needs 200 GB of available host memory ({avail / 1e9:.0f} GB here)")
+    n = (512, 512, 512)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o)
+    d = oracle_mod.DiagOutput(o.bins)
+    r_ref, f_ref = o.rhs(f, filter=1, output=1, diag=d)
+    r_gpu, f_gpu = ctx.mk_rhs(f, filter=1, output=1)
+    errs = seg_rel_err(r_gpu, r_ref, o.N, o.Next)
+    assert max(errs.values()) < 1e-11, errs
+    assert np.abs(f_gpu - f_ref).max() < 1e-13
+    g = ctx.output()
+    assert np.abs(g["gw"] - d.gw).max() <= 1e-10 * np.abs(d.gw).max()
+    ctx.close()
+    o.close()
