@@ -158,18 +158,26 @@ def _digest(params: dict) -> str:
     return h.hexdigest()[:16]
 
 
-def build(params: dict | None = None, cc: str | None = None) -> Path:
-    """Compile the reference for one parameter set; returns its directory
-    (holding main.h and libihref.so).  Cached by the parameters and sources."""
+def prepare(params: dict | None = None) -> Path:
+    """The directory of one parameter set with its main.h (rendered from the
+    staged main_template.h) and params.json."""
     stage()
     params = config() if params is None else params
     d = OUT / f"cfg_{_digest(params)}"
+    d.mkdir(parents=True, exist_ok=True)
+    if not (d / "main.h").exists():
+        (d / "main.h").write_text(render_main_h((STAGE / "main_template.h").read_text(), params))
+        (d / "params.json").write_text(json.dumps(params, indent=1))
+    return d
+
+
+def build(params: dict | None = None, cc: str | None = None) -> Path:
+    """Compile the reference for one parameter set; returns its directory
+    (holding main.h and libihref.so).  Cached by the parameters and sources."""
+    d = prepare(params)
     lib = d / "libihref.so"
     if lib.exists():
         return d
-    d.mkdir(parents=True, exist_ok=True)
-    (d / "main.h").write_text(render_main_h((STAGE / "main_template.h").read_text(), params))
-    (d / "params.json").write_text(json.dumps(params, indent=1))
     cc = cc or shutil.which("gcc") or "cc"
     inc = ["-I", str(d), "-I", str(SHIM), "-I", str(STAGE), "-I", str(HERE)]
 
@@ -202,7 +210,7 @@ def build_dropin(params: dict, gpu_lib, dropin_src, include_dir, cc: str | None 
     ``gpu_lib`` (libinstaheat_gpu.so).  Returns the executable; it reads
     INITIAL_DATAPATH and writes DATAPATH (the recorder format) in its working
     directory, like the reference's ``run``."""
-    d = build(params, cc)
+    d = prepare(params)   # the reference's own toolbox/stepper files are not needed
     gpu_lib, dropin_src = Path(gpu_lib), Path(dropin_src)
     h = hashlib.sha1(dropin_src.read_bytes() + str(gpu_lib).encode() +
                      (Path(include_dir) / "instaheat_dropin.h").read_bytes() +

@@ -145,3 +145,20 @@ def test_relinked_program_without_gpu_exits_with_the_error(oracle_mod):
     assert r.returncode != 0
     assert "Read initial data from file." in r.stdout  # the reference's set-up ran
     assert "CUDA" in r.stderr, r.stderr
+
+
+@pytest.mark.skipif(not ref.available(), reason="the reference's sources are not staged")
+@pytest.mark.parametrize("method", ["DOPRI853", "RK4"])
+def test_relinked_program_builds_with_timing(method):
+    """ENABLE_TIMING=1 (the runtime datasets of main.c:131-168) with the
+    reference's own main.h: the drop-in compiles and links for either
+    integration method (the reference's own rk4.c does not compile with it,
+    rk4.c:120-124; the relinked program does not contain it)."""
+    from instaheat_gb300 import build as libbuild
+    p = dropin.read_parameters(PARAMS / "parameters_dopri853.sh")
+    keys = {k: v for k, v in p.items()
+            if k in ref.DEFAULTS and k not in ("DATAPATH", "INITIAL_DATAPATH")}
+    keys.update(ENABLE_TIMING="1", INTEGRATION_METHOD=method)
+    exe = ref.build_dropin(ref.config(**keys), libbuild.build(), dropin.HERE / "ih_dropin.c",
+                           dropin.ROOT / "include")
+    assert exe.exists()
