@@ -21,13 +21,14 @@ const char *kernel_kind_name(int k) {
   static const char *names[KK_COUNT] = {
       "k_fft_xy",       "k_fft_zr2c",    "k_fft_zc2r",       "k_fft_x_deriv4_inv",
       "k_fft_xy_rt",    "k_fft_x_tensor", "k_fft_z_rhs_fused", "k_update_h", "k_update_phi_psi", "k_filter_spectra",
-      "k_lincomb",      "k_dopri_final", "k_gw_plane2d", "k_update_h_plane"};
+      "k_lincomb",      "k_dopri_final", "k_gw_plane2d", "k_update_h_plane",
+      "k_gw_tt_plane", "k_update_h_tt"};
   return (k >= 0 && k < KK_COUNT) ? names[k] : "unknown";
 }
 
 int kernel_kind_class(int k) {
-  if (k == KK_GW_PLANE) return 0;
-  if (k == KK_UPDATE_H_PLANE) return 1;
+  if (k == KK_GW_PLANE || k == KK_GW_TT_PLANE) return 0;
+  if (k == KK_UPDATE_H_PLANE || k == KK_UPDATE_H_TT) return 1;
   if (k <= KK_Z_RHS_FUSED) return 0;
   if (k <= KK_FILTER) return 1;
   return 2;
@@ -510,7 +511,7 @@ const char *ih_autotune_report(const ih_context *h) {
 int ih_fft_set_engine(ih_context *h, int pass, int engine) {
   CTX_CHECK(h);
   if (pass == 8) {  // plane-major tensor sources with the one-pass plane transforms
-    if (engine < 0 || engine > 2) return IH_ERR_ARG;
+    if (engine < 0 || engine > 3) return IH_ERR_ARG;
     if (engine > 0 && !gw_plane_ok(&h->c)) {
       h->c.err = "the plane transforms apply to the mixed form at 256^3 with GW on";
       return IH_ERR_ARG;

@@ -2312,12 +2312,24 @@ static int autotune_t(Ctx *c) {
   // transforms on plane-major sources
   c->gw_plane = 0;
   if (st == IH_OK && sizeof(T) == 4 && gw_plane_ok(c)) {
-    float tail[3] = {0.f, 0.f, 0.f};
+    float tail[4] = {0.f, 0.f, 0.f, 0.f};
     bool planes_usable = true;
-    for (int v = 0; v < 3 && st == IH_OK; ++v) {
+    for (int v = 0; v < 4 && st == IH_OK; ++v) {
       for (int r = 0; r <= reps && st == IH_OK; ++r) {
         if (r == 1) cudaEventRecord(e0, c->stream);
-        if (v >= 1) {
+        if (v == 3) {
+          st = gw_tt_plane(c, c->gwbuf);
+          if (st == IH_OK) st = update_h_tt(c, c->gwbuf, c->y.fl, c->ytmp.fl, c->ytmp.sc);
+          if (st != IH_OK) {  // keep the forms timed so far
+            snprintf(line, sizeof line, "gw tt planes unavailable (%s); ", c->err.c_str());
+            rep += line;
+            cudaStreamSynchronize(c->stream);
+            cudaGetLastError();
+            tail[3] = -1.f;
+            st = IH_OK;
+            break;
+          }
+        } else if (v >= 1) {
           st = gw_plane_fft(c, c->gwbuf, v);
           if (st == IH_OK) st = update_h_plane(c, c->gwbuf, c->y.fl, c->ytmp.fl, c->ytmp.sc);
           if (st != IH_OK) {  // e.g. no room for a cluster of 8: keep the row passes
@@ -2340,6 +2352,7 @@ static int autotune_t(Ctx *c) {
         }
       }
       if (st != IH_OK || !planes_usable) break;
+      if (tail[v] < 0.f) continue;
       cudaEventRecord(e1, c->stream);
       if (cudaEventSynchronize(e1) != cudaSuccess ||
           cudaEventElapsedTime(&tail[v], e0, e1) != cudaSuccess) {
@@ -2351,11 +2364,12 @@ static int autotune_t(Ctx *c) {
     }
     if (st == IH_OK && planes_usable) {
       c->gw_plane = 0;
-      for (int v = 1; v < 3; ++v)
-        if (tail[v] < tail[c->gw_plane]) c->gw_plane = v;
+      for (int v = 1; v < 4; ++v)
+        if (tail[v] >= 0.f && tail[v] < tail[c->gw_plane]) c->gw_plane = v;
       snprintf(line, sizeof line,
-               "gw tail rows %.1f us, planes %.1f us, persistent planes %.1f us; ",
-               1e3 * tail[0], 1e3 * tail[1], 1e3 * tail[2]);
+               "gw tail rows %.1f us, planes %.1f us, persistent planes %.1f us, "
+               "projected planes %.1f us; ",
+               1e3 * tail[0], 1e3 * tail[1], 1e3 * tail[2], 1e3 * tail[3]);
       rep += line;
     }
   }

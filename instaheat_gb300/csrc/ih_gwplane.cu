@@ -34,6 +34,17 @@
 // along y) into shared memory, the state's tensor segments and the outputs
 // are read and written in the reference layout (runs along kz); each thread
 // then applies the same projection and equation of motion as k_update_h.
+//
+// k_gw_tt_plane + k_update_h_tt (form 3): the projection moves into the
+// plane pass.  Each persistent cluster takes whole kz planes and streams the
+// six sources of a plane through its two buffers; after each source's x
+// transform every thread adds alpha_a S_a and beta_a S_a of its 16 modes to
+// the projected sources n0, n1 it keeps in registers (the projection is
+// linear in the S_ij, toolbox.c:363-397).  After the sixth source n0 and n1
+// are stored plane-major over the plane's slots of sources 0 and 1 (dead
+// once read), so the six sources are read once and never written back;
+// k_update_h_tt then applies the equation of motion reading the two
+// projected spectra instead of six.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -242,10 +253,14 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kPlaneThreads, 1)
   const int t = tid & 15, row = tid >> 4, col = tid >> 4;
   const int warp = tid >> 5, lane = tid & 31;
   int it = 0;
+  bool late = false;
   for (long long p = cid; p < nplanes; p += ncl, ++it) {
     const int cur = it & 1;
     float2 *buf = sm.buf[cur];
-    if (!mbar_wait_bounded(&sm.bar[cur], (unsigned)((it >> 1) & 1))) atomicExch(waitflag, 1);
+    if (!mbar_wait_bounded(&sm.bar[cur], (unsigned)((it >> 1) & 1))) {
+      atomicExch(waitflag, 1);
+      late = true;
+    }
     // y transforms of the CTA's 32 rows
     float2 v[16];
     float2 *line = buf + row * kP;
@@ -279,6 +294,12 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kPlaneThreads, 1)
     if (tid == 0 && p + 2 * ncl < nplanes) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       load_chunk(spec, M, mz, p + 2 * ncl, r, buf, &sm.bar[cur]);
+    }
+  }
+  if (late) {  // as k_gw_tt_plane: the last copy into each buffer
+    for (int q = 0; q < 2; ++q) {
+      const int last = it - 1 - ((it - 1 - q) & 1);
+      if (last >= 0) mbar_wait_bounded(&sm.bar[q], (unsigned)((last >> 1) & 1));
     }
   }
 }
@@ -342,6 +363,199 @@ __global__ void __launch_bounds__(256, 3)
       }
       C2<float> o3, o4;
       tensor_eom_core<float>(g, id, n0, n1, ksq, tc, hq[q], out, skip_pos, o3, o4);
+      mx = fmaxf(mx, fmaxf(fmaxf(fabsf(o3.x), fabsf(o3.y)), fmaxf(fabsf(o4.x), fabsf(o4.y))));
+    }
+  }
+  dh_max_store<float>(mx, outsc);
+}
+
+// n0 += alpha_a S_a, n1 += beta_a S_a over the 16 modes x = t + 16 b of
+// column y = yj of plane kz (v[b] = S_a there)
+__device__ __forceinline__ void tt_accumulate(const Geom &g, int a, int t, int ja, float ky, int kz,
+                                              int yj, const float2 (&v)[16], float2 (&n0)[16],
+                                              float2 (&n1)[16]) {
+  const float kzf = (float)g.kzu * (float)kz;
+  const float kzz = (float)g.kz2 * (float)kz * (float)kz;
+  const float kyy = (float)g.ky2 * (float)ja * (float)ja;
+  const int branch = kz != 0 ? 0 : (yj != 0 ? 1 : 2);
+#pragma unroll
+  for (int b = 0; b < 16; ++b) {
+    const int xi = t + 16 * b;
+    const int ia = xi > kP / 2 ? kP - xi : xi;
+    const float kx = (float)g.kxu * (float)(xi > kP / 2 ? xi - kP : xi);
+    float ksq = kzz;
+    ksq += (float)g.kx2 * (float)ia * (float)ia;
+    ksq += kyy;
+    const float inv = ksq > 0.f ? 1.f / ksq : 0.f;
+    float al, be;
+    tensor_coef<float>(a, branch, kx, ky, kzf, kx * inv, ky * inv, kzf * inv, al, be);
+    n0[b].x += al * v[b].x;
+    n0[b].y += al * v[b].y;
+    n1[b].x += be * v[b].x;
+    n1[b].y += be * v[b].y;
+  }
+}
+
+// Form 3, pass 1: y and x transforms of the six sources of each kz plane
+// and their TT projection.  Cluster c takes planes kz = c, c + C, ... (C
+// resident clusters); its iteration it handles source a = it % 6 of plane
+// kz = c + (it / 6) C, in buffer it % 2, with the load of iteration it + 2
+// issued as soon as the buffer is free.  Thread (column j = tid / 16, t =
+// tid % 16) of CTA r ends each x transform with the modes x = t + 16 b,
+// y = 32 r + j, b = 0..15, and keeps n0, n1 of those 16 modes in registers
+// across the six sources.
+__global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kPlaneThreads, 1)
+    k_gw_tt_plane(float2 *spec, Geom g, const float2 *__restrict__ twg, int *waitflag) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  PlaneSmem2 &sm = *reinterpret_cast<PlaneSmem2 *>(smraw);
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const int tid = threadIdx.x;
+  const int mz = g.mz;
+  const long long M = g.M;
+  const int cid = (int)(blockIdx.x / kCl), ncl = (int)(gridDim.x / kCl);
+  const int nloc = cid < mz ? (mz - 1 - cid) / ncl + 1 : 0;  // planes of this cluster
+  const int nit = 6 * nloc;
+  if (tid == 0) {
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
+    for (int q = 0; q < 2 && q < nit; ++q)
+      load_chunk(spec, M, mz, (long long)q * mz + cid, r, sm.buf[q], &sm.bar[q]);
+  }
+  for (int i = tid; i < kP; i += kPlaneThreads) sm.tw[i] = twg[i];
+  __syncthreads();
+  const int t = tid & 15, row = tid >> 4;  // y pass: row x = 32 r + row; x pass: column y
+  const int warp = tid >> 5, lane = tid & 31;
+  const int yj = r * kRows + row;
+  const int ja = yj > kP / 2 ? kP - yj : yj;
+  const float ky = (float)g.kyu * (float)(yj > kP / 2 ? yj - kP : yj);
+  float2 n0[16], n1[16];
+  bool late = false;  // a wait gave up: the results are void (waitflag set)
+  for (int it = 0; it < nit; ++it) {
+    const int cur = it & 1, a = it % 6;
+    const int kz = cid + (it / 6) * ncl;
+    float2 *buf = sm.buf[cur];
+    if (a == 0) {
+#pragma unroll
+      for (int b = 0; b < 16; ++b) n0[b] = n1[b] = make_float2(0.f, 0.f);
+    }
+    if (!mbar_wait_bounded(&sm.bar[cur], (unsigned)((it >> 1) & 1))) {
+      atomicExch(waitflag, 1);
+      late = true;
+    }
+    // y transforms of the CTA's 32 rows
+    float2 v[16];
+    float2 *line = buf + row * kP;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = line[t + 16 * m];
+    __syncwarp();
+    line_fft256(v, t, line, 1, sm.tw);
+    cluster.sync();  // every CTA is done with its rows: the buffers take column tiles
+    const int x = r * kRows + row;
+#pragma unroll
+    for (int b = 0; b < 16; ++b) {
+      float2 *dst = cluster.map_shared_rank(buf, b >> 1);
+      dst[x * kLd + t + 16 * (b & 1)] = v[b];
+    }
+    cluster.sync();  // the column tiles are complete
+    // x transforms of the CTA's 32 columns
+    float2 *cline = buf + row;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = cline[(t + 16 * m) * kLd];
+    __syncwarp();
+    line_fft256(v, t, cline, kLd, sm.tw);
+    __syncthreads();  // every read of buf is done
+    if (a < 5 && tid == 0 && it + 2 < nit) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      const int i2 = it + 2;
+      load_chunk(spec, M, mz, (long long)(i2 % 6) * mz + cid + (i2 / 6) * ncl, r, buf,
+                 &sm.bar[cur]);
+    }
+    // the projection of source a (coefficients as k_fft_x_tensor, FP32)
+    tt_accumulate(g, a, t, ja, ky, kz, yj, v, n0, n1);
+    if (a == 5) {
+      // n0 then n1, transposed through buf (free: its next load is not yet
+      // issued), over the plane's slots of sources 0 and 1: rows of 32 y
+      const bool zero_mode = kz == 0 && yj == 0 && t == 0;  // x = y = kz = 0: no sources
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+#pragma unroll
+        for (int b = 0; b < 16; ++b) {
+          float2 w = s == 0 ? n0[b] : n1[b];
+          if (b == 0 && zero_mode) w = make_float2(0.f, 0.f);
+          buf[(t + 16 * b) * kLd + row] = w;
+        }
+        __syncthreads();
+        float2 *o = spec + (long long)s * M + (long long)kz * kP * kP + r * kRows + lane;
+#pragma unroll 4
+        for (int xr = warp; xr < kP; xr += kPlaneThreads / 32)
+          o[(long long)xr * kP] = buf[xr * kLd + lane];
+        __syncthreads();
+      }
+      if (tid == 0 && it + 2 < nit) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const int i2 = it + 2;
+        load_chunk(spec, M, mz, (long long)(i2 % 6) * mz + cid + (i2 / 6) * ncl, r, buf,
+                   &sm.bar[cur]);
+      }
+    }
+  }
+  // after a wait that gave up, wait (bounded) once more for the last copy
+  // into each buffer before the CTA's shared memory is released
+  if (late) {
+    for (int q = 0; q < 2; ++q) {
+      const int last = nit - 1 - ((nit - 1 - q) & 1);
+      if (last >= 0) mbar_wait_bounded(&sm.bar[q], (unsigned)((last >> 1) & 1));
+    }
+  }
+}
+
+// Form 3, pass 2: the equation of motion from the projected sources n0, n1
+// (plane-major, sources 0 and 1 of spec) over tiles of one x row, 32 y and
+// 32 kz, as k_update_h_plane without the projection.
+struct UhTtSmem {
+  float2 s[2][kTileK][kTileY + 1];
+};
+
+__global__ void __launch_bounds__(256, 4)
+    k_update_h_tt(const float2 *__restrict__ spec, const float *__restrict__ y,
+                  float *__restrict__ out, const RhsScalars *rs, Geom g, int skip_pos,
+                  double *outsc) {
+  __shared__ UhTtSmem sm;
+  const int x = blockIdx.x;
+  const int y0 = blockIdx.y * kTileY;
+  const int k0 = blockIdx.z * kTileK;
+  const int nk = min(kTileK, g.mz - k0);
+  const long long M = g.M;
+  const long long plane = (long long)g.nx * g.ny;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int q = warp; q < 2 * nk; q += 8) {
+    const int a = q / nk, kl = q - a * nk;
+    sm.s[a][kl][lane] =
+        spec[(long long)a * M + (long long)(k0 + kl) * plane + (long long)x * g.ny + y0 + lane];
+  }
+  __syncthreads();
+  const TensorConsts<float> tc(rs);
+  float mx = 0.f;
+  const int kl = lane;
+  if (kl < nk) {
+    const int kz = k0 + kl;
+    HVals<float> hq[kTileY / 8];
+#pragma unroll
+    for (int q = 0; q < kTileY / 8; ++q)
+      tensor_load<float>(g, ((long long)x * g.ny + y0 + warp + 8 * q) * g.mz + kz, y, hq[q]);
+#pragma unroll
+    for (int q = 0; q < kTileY / 8; ++q) {
+      const int yl = warp + 8 * q;
+      const long long id = ((long long)x * g.ny + y0 + yl) * g.mz + kz;
+      Mode m;
+      m.i = x;
+      m.j = y0 + yl;
+      m.k = kz;
+      const float ksq = id != 0 ? mode_k<float>(g, m).ksq : 0.f;
+      C2<float> o3, o4;
+      tensor_eom_core<float>(g, id, sm.s[0][kl][yl], sm.s[1][kl][yl], ksq, tc, hq[q], out,
+                             skip_pos, o3, o4);
       mx = fmaxf(mx, fmaxf(fmaxf(fabsf(o3.x), fabsf(o3.y)), fmaxf(fabsf(o4.x), fabsf(o4.y))));
     }
   }
@@ -412,6 +626,52 @@ int update_h_plane(Ctx *c, const void *spec, const void *y, void *out, double *o
   return check_launch(c, "k_update_h_plane");
 }
 
+// the clusters of 8 that can be resident at once (the persistent grid)
+static int resident_clusters(const void *kernel, size_t smem, cudaStream_t s, int *ncl) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kCl * 64, 1, 1);
+  cfg.blockDim = dim3(kPlaneThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  *ncl = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveClusters(ncl, kernel, &cfg);
+  return e == cudaSuccess && *ncl >= 1 ? IH_OK : IH_ERR_CUDA;
+}
+
+int gw_tt_plane(Ctx *c, void *spec) {
+  const Geom &g = c->g;
+  const size_t smem = sizeof(PlaneSmem2);
+  IH_CUDA(c, cudaFuncSetAttribute(k_gw_tt_plane, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+  if (c->gw_tt_clusters <= 0) {
+    int ncl = 0;
+    if (resident_clusters((const void *)k_gw_tt_plane, smem, c->stream, &ncl) != IH_OK) {
+      c->err = "no cluster of 8 CTAs of k_gw_tt_plane fits the device";
+      return IH_ERR_CUDA;
+    }
+    c->gw_tt_clusters = ncl;
+  }
+  const int ncl = c->gw_tt_clusters < g.mz ? c->gw_tt_clusters : g.mz;
+  prof_begin(c, KK_GW_TT_PLANE);
+  k_gw_tt_plane<<<(unsigned)(ncl * kCl), kPlaneThreads, smem, c->stream>>>(
+      reinterpret_cast<float2 *>(spec), g, reinterpret_cast<const float2 *>(c->tw_z), c->waitflag);
+  prof_end(c, KK_GW_TT_PLANE, 8.0 * g.M * sizeof(float2));
+  return check_launch(c, "k_gw_tt_plane");
+}
+
+int update_h_tt(Ctx *c, const void *spec, const void *y, void *out, double *outsc) {
+  const Geom &g = c->g;
+  dim3 grid((unsigned)g.nx, (unsigned)(g.ny / kTileY), (unsigned)((g.mz + kTileK - 1) / kTileK));
+  prof_begin(c, KK_UPDATE_H_TT);
+  k_update_h_tt<<<grid, 256, 0, c->stream>>>(reinterpret_cast<const float2 *>(spec),
+                                             reinterpret_cast<const float *>(y),
+                                             reinterpret_cast<float *>(out), c->rs, g, c->skip_pos,
+                                             outsc);
+  prof_end(c, KK_UPDATE_H_TT,
+           2.0 * g.M * sizeof(float2) + (c->skip_pos ? 6.0 : 8.0) * g.Next * sizeof(float));
+  return check_launch(c, "k_update_h_tt");
+}
+
 }  // namespace ih
 
 // ---------------------------------------------------------------------------
@@ -421,7 +681,7 @@ int update_h_plane(Ctx *c, const void *spec, const void *y, void *out, double *o
 // counterpart.
 extern "C" int ih_gw_plane_probe(int device, int form, int mz, int reps, double *ms_per_launch) {
   using namespace ih;
-  if (!ms_per_launch || reps < 1 || mz < 1 || (form != 1 && form != 2)) return IH_ERR_ARG;
+  if (!ms_per_launch || reps < 1 || mz < 1 || form < 1 || form > 3) return IH_ERR_ARG;
   if (cudaSetDevice(device) != cudaSuccess) return IH_ERR_CUDA;
   const long long M = (long long)kP * kP * mz, nplanes = 6LL * mz;
   float2 *buf = nullptr, *tw = nullptr;
@@ -431,6 +691,16 @@ extern "C" int ih_gw_plane_probe(int device, int form, int mz, int reps, double 
   float ms = 0.f;
   int ncl = 0;
   float2 htw[kP];
+  // k vectors of a 256 x 256 x 2(mz - 1) grid in a box of 20 (form 3's
+  // projection; they change the arithmetic, not the memory traffic)
+  Geom g = {};
+  g.nx = g.ny = kP;
+  g.nz = 2 * (mz - 1);
+  g.h = mz - 1;
+  g.mz = mz;
+  g.M = M;
+  g.kxu = g.kyu = g.kzu = kTwoPi / 20.0;
+  g.kx2 = g.ky2 = g.kz2 = g.kxu * g.kxu;
   for (int k = 0; k < kP; ++k) {
     const double ang = 6.283185307179586476925286766559 * k / kP;
     htw[k] = make_float2((float)cos(ang), (float)-sin(ang));
@@ -445,22 +715,23 @@ extern "C" int ih_gw_plane_probe(int device, int form, int mz, int reps, double 
   if (cudaFuncSetAttribute(k_gw_plane2d, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)sizeof(PlaneSmem)) != cudaSuccess ||
       cudaFuncSetAttribute(k_gw_plane2p, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sizeof(PlaneSmem2)) != cudaSuccess ||
+      cudaFuncSetAttribute(k_gw_tt_plane, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)sizeof(PlaneSmem2)) != cudaSuccess)
     goto done;
-  if (form == 2) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(kCl * 64, 1, 1);
-    cfg.blockDim = dim3(kPlaneThreads, 1, 1);
-    cfg.dynamicSmemBytes = sizeof(PlaneSmem2);
-    if (cudaOccupancyMaxActiveClusters(&ncl, (const void *)k_gw_plane2p, &cfg) != cudaSuccess ||
-        ncl < 1)
+  if (form >= 2) {
+    if (resident_clusters(form == 2 ? (const void *)k_gw_plane2p : (const void *)k_gw_tt_plane,
+                          sizeof(PlaneSmem2), 0, &ncl) != IH_OK)
       goto done;
-    if (ncl > nplanes) ncl = (int)nplanes;
+    const long long units = form == 2 ? nplanes : mz;
+    if (ncl > units) ncl = (int)units;
   }
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) goto done;
   for (int r = 0; r <= reps; ++r) {  // r = 0: warm-up
     if (r == 1) cudaEventRecord(e0);
-    if (form == 2)
+    if (form == 3)
+      k_gw_tt_plane<<<(unsigned)(ncl * kCl), kPlaneThreads, sizeof(PlaneSmem2)>>>(buf, g, tw, flag);
+    else if (form == 2)
       k_gw_plane2p<<<(unsigned)(ncl * kCl), kPlaneThreads, sizeof(PlaneSmem2)>>>(buf, M, mz, nplanes,
                                                                                 tw, flag);
     else

@@ -113,6 +113,8 @@ enum KernelKind {
   KK_DOPRI_FINAL,       // field_new + embedded error sums
   KK_GW_PLANE,          // y and x transforms of the tensor sources, one kz plane per cluster
   KK_UPDATE_H_PLANE,    // update_h reading plane-major tensor sources
+  KK_GW_TT_PLANE,       // tensor sources' y/x transforms + TT projection, persistent clusters
+  KK_UPDATE_H_TT,       // tensor equation of motion from the projected sources
   KK_COUNT
 };
 const char *kernel_kind_name(int k);
@@ -224,8 +226,10 @@ struct Ctx {
   int rt_var[2] = {FV_TWOSTEP_HALF, FV_TWOSTEP_HALF};  // x, y round trips (two-step forms)
   int roundtrip = 1;  // RHS without filter/output: round trips instead of full spectra
   int tensor_fused = 0;  // update_h fused into the last x pass (autotuner's choice)
-  int gw_plane = 0;      // tensor sources plane-major: 1 one cluster per plane, 2 persistent
+  int gw_plane = 0;      // tensor sources plane-major: 1 one cluster per plane, 2 persistent,
+                         // 3 persistent with the projection (k_gw_tt_plane + k_update_h_tt)
   int gw_clusters = 0;   // resident clusters of the persistent plane transforms
+  int gw_tt_clusters = 0;  // resident clusters of k_gw_tt_plane
   int *waitflag = nullptr;  // device int: a bounded device-side wait timed out
   void *gwbuf = nullptr;    // plane-major tensor sources: 6 spectra of M complex (T)
   int zwide = 1;         // the wide-row fused z pass where it applies (nz = 256, mixed)
@@ -328,6 +332,8 @@ int fused_wide_launch(Ctx *c, const void *d4, const void *yfl, const double *ysc
 bool gw_plane_ok(const Ctx *c);
 int gw_plane_fft(Ctx *c, void *spec, int form);
 int update_h_plane(Ctx *c, const void *spec, const void *y, void *out, double *outsc);
+int gw_tt_plane(Ctx *c, void *spec);
+int update_h_tt(Ctx *c, const void *spec, const void *y, void *out, double *outsc);
 
 int fft_tables(Ctx *c);
 // time every engine variant of the x/y passes and the fused x pass on the

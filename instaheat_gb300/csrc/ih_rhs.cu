@@ -1093,7 +1093,10 @@ static int rhs_t(Ctx *c, Vec &y, Vec &k, int filter, int output, const Vec *smry
     // S_ij spectra: spec[0..3] and spec[5..6]; forward y and x passes
     // (batched: per-array y-then-x ordering measured slower, no L2 reuse;
     // kz slabs of all six arrays where the autotuner chose them)
-    if (plane) {
+    if (plane && c->gw_plane == 3) {
+      IH_TRY(gw_tt_plane(c, c->gwbuf));
+      IH_TRY(update_h_tt(c, c->gwbuf, yfl, kfl, k.sc));
+    } else if (plane) {
       IH_TRY(gw_plane_fft(c, c->gwbuf, c->gw_plane));
       IH_TRY(update_h_plane(c, c->gwbuf, yfl, kfl, k.sc));
     } else if (c->gw_slab > 0 && !c->tensor_fused && g.pow2) {

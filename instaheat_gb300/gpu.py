@@ -180,7 +180,8 @@ def load(build_if_missing: bool = True):
 
 def gw_plane_probe(form, mz=129, reps=20, device=0) -> float:
     """Milliseconds per launch of the tensor sources' plane transforms alone
-    (ih_gw_plane_probe; form 1 one cluster per plane, 2 persistent)."""
+    (ih_gw_plane_probe; form 1 one cluster per plane, 2 persistent, 3 persistent
+    with the TT projection)."""
     v = C.c_double()
     st = load().ih_gw_plane_probe(device, form, mz, reps, C.byref(v))
     if st != 0:

@@ -650,7 +650,7 @@ def test_dopri853_f64_to_t10(gpu_mod, oracle_mod):
     o.close()
 
 
-@pytest.mark.parametrize("form", [1, 2])
+@pytest.mark.parametrize("form", [1, 2, 3])
 def test_mixed_gw_planes_match_rows(gpu_mod, oracle_mod, form):
     """The tensor sources plane-major (one cluster per kz plane transforms it
     along y and x through distributed shared memory; update_h reads the
@@ -659,7 +659,9 @@ def test_mixed_gw_planes_match_rows(gpu_mod, oracle_mod, form):
     the other segments identical; against the FP64 oracle's tensor RHS
     within the mixed form's tolerance (1e-4 of the segment magnitude).
     Form 1: one cluster per plane; form 2: persistent clusters prefetching
-    the next plane."""
+    the next plane; form 3: persistent clusters over whole kz planes that
+    accumulate the TT projection of the six sources (update_h reads the two
+    projected spectra)."""
     n = (256, 256, 256)
     ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
     o = oracle_mod.Oracle(n=n)
@@ -682,7 +684,7 @@ def test_mixed_gw_planes_match_rows(gpu_mod, oracle_mod, form):
     o.close()
 
 
-@pytest.mark.parametrize("form", [1, 2])
+@pytest.mark.parametrize("form", [1, 2, 3])
 def test_mixed_gw_planes_dopri_steps(gpu_mod, oracle_mod, form):
     """Three mixed-form DOPRI853 steps at 256^3 with the plane-major tensor
     sources track the row/column form (same accepted steps to 1e-6, state
