@@ -435,6 +435,19 @@ def reference_arm(args, dist):
 
 # ------------------------------------------------------------ study legs
 
+def plane_probe(gpu, forms, reps):
+    """The tensor sources' plane pass (ih_fft_set_engine pass 8 forms) alone
+    on six 256 x 256 x 129 complex FP32 spectra (405 MB): ms per launch and
+    the rate of its algorithmic bytes (forms 1, 2: the six spectra read and
+    written; form 3: read, and the two projected spectra written)."""
+    M = 256 * 256 * 129
+    for form in forms:
+        ms = gpu.gw_plane_probe(form, 129, max(1, reps))
+        nbytes = (12 if form < 3 else 8) * M * 8
+        print(json.dumps({"form": form, "ms": ms, "bytes": nbytes,
+                          "GBs": nbytes / (ms * 1e-3) / 1e9}), flush=True)
+
+
 def case_workload(gpu, args):
     """K RHS evaluations or DOPRI853 steps of the seeded workload (the
     program the ncu captures under profiles/ run)."""
@@ -553,9 +566,11 @@ def long_run(gpu, n, checkpoints, forms, seed, rtol, device=0, L=L_BOX, phi0=1.0
         ctx = gpu.Context(n=(n,) * 3, L=(L,) * 3, precision=prec, device=device, autotune=True)
         ctx.ic(seed=seed, amp=AMP, phi0=phi0)
         ctx.dopri_init(gpu.dopri_cfg(rtol, rtol), 0.0, 1e-3)
-        if form == "mixed_learned":
+        if form in ("mixed_learned", "mixed_learned_cap"):
             mlp, _ = learned_dt.load(model or learned_dt.DEFAULT_MODEL, device=device)
             ctx.set_proposer(mlp)
+            if form == "mixed_learned_cap":
+                ctx.set_proposer_policy(gpu.PROPOSER_CAP)
         wall, steps_all = 0.0, 0
         res[form] = []
         for tc in checkpoints:
@@ -653,10 +668,11 @@ def config_run(which, seed=0):
                           "calls_rhs": float(got["calls_rhs"][0])}}
     for k in ("runtime_stepper",):
         if k in want and k in got:
-            out["reference"][k + "_s"] = float(want[k][0])
-            out["dropin_gpu"][k + "_s"] = float(got[k][0])
-            out["reference"]["mt_per_s_stepper"] = span / float(want[k][0])
-            out["dropin_gpu"]["mt_per_s_stepper"] = span / float(got[k][0])
+            for side, d in (("reference", want), ("dropin_gpu", got)):
+                v = float(d[k][0])
+                out[side][k + "_s"] = v
+                if v > 0:
+                    out[side]["mt_per_s_stepper"] = span / v
     for k in ("steps_total", "steps_ok", "steps_bad"):
         if k in want:
             out[k] = {"reference": float(want[k][0]), "dropin_gpu": float(got[k][0])}
@@ -712,6 +728,8 @@ def main():
     ap.add_argument("--box", type=float, default=L_BOX)
     ap.add_argument("--phi0", type=float, default=1.0)
     ap.add_argument("--model", default=None, help="proposer model file (default: the committed one)")
+    ap.add_argument("--plane-probe", default=None,
+                    help="comma-separated forms of the tensor sources' plane pass, timed alone")
     ap.add_argument("--config-run", type=int, default=0, choices=[0, 1, 2],
                     help="configuration 1 or 2 through the reference program and the relinked one")
     args = ap.parse_args()
@@ -724,6 +742,8 @@ def main():
     build.build()
     if args.case_rhs or args.case_steps:
         return case_workload(gpu, args)
+    if args.plane_probe:
+        return plane_probe(gpu, [int(x) for x in args.plane_probe.split(",")], args.steps)
     if args.dt_study is not None:
         return dt_study(gpu, args.grid, [float(x) for x in args.dt_study.split(",")], args.rtol)
     if args.gw_accuracy > 0:

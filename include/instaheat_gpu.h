@@ -201,8 +201,11 @@ const char *ih_autotune_report(const ih_context *c);
  * buffer of their own, one cluster of 8 CTAs transforms a plane along y and x
  * in one pass through distributed shared memory, and update_h reads the
  * planes; 2: the same with persistent clusters that load the next plane
- * while they transform the current one; mixed form at 256^3 only,
- * IH_ERR_ARG elsewhere; 0: the row and column passes);
+ * while they transform the current one; 3: persistent clusters that take
+ * whole kz planes, transform the six sources of a plane one after the other
+ * and accumulate their TT projection, so that update_h reads two projected
+ * spectra instead of six; mixed form at 256^3 only, IH_ERR_ARG elsewhere;
+ * 0: the row and column passes);
  * engine IH_FFT_STOCKHAM, IH_FFT_TWOSTEP (register two-step,
  * 128-byte tiles), IH_FFT_TWOSTEP_HALF (64-byte tiles), IH_FFT_PIPELINED
  * (register two-step in persistent CTAs that copy the next tile in with
@@ -358,6 +361,14 @@ int ih_mlp_train(ih_mlp *m, const float *x, const float *y, int n, int iters, in
 int ih_step_features(ih_context *c, float *out12);
 /* set (or with NULL clear) the proposer of a context */
 int ih_dopri853_set_proposer(ih_context *c, ih_mlp *m);
+/* How the proposal is used: IH_PROPOSER_CLAMPED (0, the default) -- the
+ * proposal clamped as above; IH_PROPOSER_CAP (1) -- the same, except that
+ * after a step whose controller proposal is the Hubble cap itself
+ * (dopri853.c:525-530) the next step is the cap: the proposer then only
+ * shortens steps the error controller sets. */
+#define IH_PROPOSER_CLAMPED 0
+#define IH_PROPOSER_CAP 1
+int ih_dopri853_set_proposer_policy(ih_context *c, int policy);
 
 /* ---- ensembles (no reference counterpart: the reference runs one
  * realization per process) ----
@@ -446,7 +457,8 @@ int ih_host_free(void *p);
  * plain FP64 form. */
 int ih_fp64_fma_peak(int device, int iters, int reps, double *tflops);
 /* The tensor sources' plane transforms (ih_fft_set_engine pass 8: form 1 one
- * cluster per plane, 2 persistent clusters) alone on a zeroed buffer of six
+ * cluster per plane, 2 persistent clusters, 3 persistent clusters with the
+ * TT projection, k vectors of a box of 20) alone on a zeroed buffer of six
  * 256 x 256 x mz complex FP32 spectra (mz = 129 at 256^3: 405 MB), `reps`
  * CUDA-event-timed launches after one warm-up: milliseconds per launch. */
 int ih_gw_plane_probe(int device, int form, int mz, int reps, double *ms_per_launch);

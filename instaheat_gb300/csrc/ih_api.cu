@@ -858,6 +858,13 @@ int ih_dopri853_set_proposer(ih_context *h, ih_mlp *m) {
   return IH_OK;
 }
 
+int ih_dopri853_set_proposer_policy(ih_context *h, int policy) {
+  CTX_CHECK(h);
+  if (policy != IH_PROPOSER_CLAMPED && policy != IH_PROPOSER_CAP) return IH_ERR_ARG;
+  h->c.proposer_policy = policy;
+  return IH_OK;
+}
+
 int ih_prepare_output(ih_context *h) {
   CTX_CHECK(h);
   Ctx *c = &h->c;

@@ -199,6 +199,7 @@ struct Ctx {
   double hist_dt[4] = {0, 0, 0, 0}, hist_err[4] = {0, 0, 0, 0};
   int hist_n = 0;
   ih_mlp *proposer = nullptr;
+  int proposer_policy = 0;  // IH_PROPOSER_CLAMPED or IH_PROPOSER_CAP
   float *feat_dev = nullptr;    // 16 floats: 12 features, output at [12]
   double dt_next_pi = 0.0;      // the controller's own proposal of the last step
 

@@ -902,8 +902,12 @@ static int learned_dt(Ctx *c, double dt_did, double rho_mean, double *dt_out) {
   double dt = exp((double)ylog);
   if (!(dt > 0.0) || !isfinite(dt)) dt = c->dt_next_pi;  // fall back to the controller
   dt = fmin(fmax(dt, dt_did * c->cfg.minscale), dt_did * c->cfg.maxscale);
-  if (c->cfg.max_dt_hubble_fraction > 0.0)
-    dt = fmin(dt, c->cfg.max_dt_hubble_fraction * sqrt(3.0 / rho_mean));
+  if (c->cfg.max_dt_hubble_fraction > 0.0) {
+    // success() caps dt_next_pi with the same expression, so the comparison
+    // is exact where the controller sits on the cap
+    const double cap = c->cfg.max_dt_hubble_fraction * sqrt(3.0 / rho_mean);
+    dt = (c->proposer_policy == IH_PROPOSER_CAP && c->dt_next_pi >= cap) ? cap : fmin(dt, cap);
+  }
   *dt_out = dt;
   return IH_OK;
 }

@@ -345,6 +345,7 @@ static void mk_power_spectrum(const iho_ctx *c, const double *in, double *out)
         double p2 = in[2 * i] * in[2 * i] + in[2 * i + 1] * in[2 * i + 1];
         if (fabs(c->kz[i]) > DBL_EPSILON) p2 *= 2.0;
         size_t idx = (int)trunc(bins * sqrt(c->ksq[i]) / c->kmax - 1.0e-14);
+        if (idx >= (size_t)bins) idx = bins - 1;  /* |k| = k_max: see mk_gw_spectrum */
         out[idx] += p2 / c->N;
     }
 }
@@ -421,6 +422,12 @@ static void mk_gw_spectrum(const iho_ctx *c, const double *f, double *gw)
         }
         if (fabs(c->kz[i]) > DBL_EPSILON) pw *= 2.0;
         size_t idx = (int)trunc(bins * k / c->kmax - 1.0e-14);
+        /* The - 1e-14 of toolbox.c:479 puts |k| = k_max (the grid corner) into
+         * the last bin; where bins * k / k_max rounds to exactly `bins` (e.g.
+         * 512^3 with 256 bins) the subtraction is lost to rounding and
+         * toolbox.c writes one past its array.  The corner mode is kept in
+         * the last bin here, as the offset intends (the GPU does the same). */
+        if (idx >= (size_t)bins) idx = bins - 1;
         gw[idx] += fac * k2 * k * pw;
     }
     for (int i = 0; i < bins; ++i) gw[i] /= N;

@@ -159,7 +159,10 @@ class NumpyRHS:
         return n0, n1
 
     def _bin_index(self, k):
-        return np.trunc(self.bins * k / self.kmax - 1.0e-14).astype(int)
+        # |k| = k_max stays in the last bin where the offset is lost to
+        # rounding (toolbox.c:479 would index one past its array there)
+        return np.minimum(np.trunc(self.bins * k / self.kmax - 1.0e-14).astype(int),
+                          self.bins - 1)
 
     def power_spectrum(self, c):
         p2 = (np.abs(c) ** 2).ravel().copy()
