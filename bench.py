@@ -566,11 +566,9 @@ def long_run(gpu, n, checkpoints, forms, seed, rtol, device=0, L=L_BOX, phi0=1.0
         ctx = gpu.Context(n=(n,) * 3, L=(L,) * 3, precision=prec, device=device, autotune=True)
         ctx.ic(seed=seed, amp=AMP, phi0=phi0)
         ctx.dopri_init(gpu.dopri_cfg(rtol, rtol), 0.0, 1e-3)
-        if form in ("mixed_learned", "mixed_learned_cap"):
+        if form == "mixed_learned":
             mlp, _ = learned_dt.load(model or learned_dt.DEFAULT_MODEL, device=device)
             ctx.set_proposer(mlp)
-            if form == "mixed_learned_cap":
-                ctx.set_proposer_policy(gpu.PROPOSER_CAP)
         wall, steps_all = 0.0, 0
         res[form] = []
         for tc in checkpoints:

@@ -190,9 +190,11 @@ const char *ih_autotune_report(const ih_context *c);
 /* Pin or read the engine of one pass: pass 0 = x, 1 = y, 2 = the fused
  * inverse x pass, 3 / 4 = the x / y derivative round trips (two-step forms
  * only), 5 = the last x pass of the tensor sources (0 = x passes then
- * update_h, 1 = one kernel accumulating the TT projection), 6 = the fused z
- * pass of the RHS (1 = the wide-row engine, 8 lanes x 16 values per row, where
- * it applies: mixed form, nz = 256 -- the default; 0 = a warp per row), 7 =
+ * update_h, 1 = one kernel accumulating the TT projection), 6 = the z passes
+ * of the RHS at nz = 256 (1 = the wide-row engine, 8 lanes x 16 values per
+ * row, both precisions -- the default; 2 = the same, each row's next input
+ * spectrum copied into shared memory with cp.async during the current
+ * transform, mixed form only; 0 = a warp per row), 7 =
  * the kz slab width of the forward y and x passes of the six tensor sources
  * (0 = whole arrays, the default; a multiple of 8 up to 64 = y then x pass on
  * one slab of all six at a time, so the slab stays in L2 between the two; it
@@ -361,14 +363,6 @@ int ih_mlp_train(ih_mlp *m, const float *x, const float *y, int n, int iters, in
 int ih_step_features(ih_context *c, float *out12);
 /* set (or with NULL clear) the proposer of a context */
 int ih_dopri853_set_proposer(ih_context *c, ih_mlp *m);
-/* How the proposal is used: IH_PROPOSER_CLAMPED (0, the default) -- the
- * proposal clamped as above; IH_PROPOSER_CAP (1) -- the same, except that
- * after a step whose controller proposal is the Hubble cap itself
- * (dopri853.c:525-530) the next step is the cap: the proposer then only
- * shortens steps the error controller sets. */
-#define IH_PROPOSER_CLAMPED 0
-#define IH_PROPOSER_CAP 1
-int ih_dopri853_set_proposer_policy(ih_context *c, int policy);
 
 /* ---- ensembles (no reference counterpart: the reference runs one
  * realization per process) ----

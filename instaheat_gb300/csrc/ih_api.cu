@@ -530,7 +530,8 @@ int ih_fft_set_engine(ih_context *h, int pass, int engine) {
   if (pass == 2 && (engine == FV_THREESTEP || engine == FV_TWOSTEP_HALF_OCC)) return IH_ERR_ARG;
   if ((pass == 3 || pass == 4) && engine != FV_TWOSTEP && engine != FV_TWOSTEP_HALF)
     return IH_ERR_ARG;
-  if (pass >= 5 && engine > 1) return IH_ERR_ARG;
+  if (pass == 5 && engine > 1) return IH_ERR_ARG;
+  if (pass == 6 && (engine > 2 || (engine == 2 && !h->c.mixed))) return IH_ERR_ARG;
   if (pass < 2) {
     h->c.xy_var[pass] = engine;
   } else if (pass == 2) {
@@ -855,13 +856,6 @@ int ih_dopri853_set_proposer(ih_context *h, ih_mlp *m) {
   Ctx *c = &h->c;
   if (m && !c->feat_dev) IH_TRY(dmalloc(c, (void **)&c->feat_dev, sizeof(float) * 16));
   c->proposer = m;
-  return IH_OK;
-}
-
-int ih_dopri853_set_proposer_policy(ih_context *h, int policy) {
-  CTX_CHECK(h);
-  if (policy != IH_PROPOSER_CLAMPED && policy != IH_PROPOSER_CAP) return IH_ERR_ARG;
-  h->c.proposer_policy = policy;
   return IH_OK;
 }
 

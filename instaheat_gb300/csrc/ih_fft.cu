@@ -472,25 +472,8 @@ __global__ void __launch_bounds__(threads3<L, B>()) k_fft_xy_3s(C2<T> *data, lon
 // engines idle their loads during the arithmetic).  The tile buffer is
 // [L][B] without padding -- a row is one 128-byte line (or half), so the
 // line-wise accesses of both steps are free of bank conflicts -- and after
-// step 1 has read it into registers it is reused for the exchange.
-template <typename T>
-__device__ __forceinline__ void cp_async_c(C2<T> *s, const C2<T> *g, bool valid) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
-  if constexpr (sizeof(T) == 4) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(g),
-                 "r"(valid ? 8 : 0)
-                 : "memory");
-  } else {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(g),
-                 "r"(valid ? 16 : 0)
-                 : "memory");
-  }
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
+// step 1 has read it into registers it is reused for the exchange (the
+// cp.async helpers are in ih_fftcore.cuh).
 
 // tile t of a pass -> its first element and the valid pencils of the tile
 struct XYTiles {
@@ -1825,9 +1808,8 @@ int fft_zr2c(Ctx *c, const T *in, long long in_stride, C2<T> *out, long long out
              int count) {
   const Geom &g = c->g;
   prof_begin(c, KK_FFT_ZR2C);
-  if (sizeof(T) == 4 && fused_wide_ok(c)) {
-    IH_TRY(zr2c_wide_launch(c, reinterpret_cast<const float *>(in), in_stride, out, out_stride,
-                            count));
+  if (fused_wide_ok(c)) {
+    IH_TRY(zr2c_wide_launch(c, in, in_stride, out, out_stride, count));
   } else if (g.h & (g.h - 1)) {
     const long long rows = (long long)g.nx * g.ny;
     const size_t sm = zg_smem<T>(g.h);
@@ -2117,7 +2099,7 @@ int fft_z_rhs_fused(Ctx *c, const C2<T> *d4, const T *yfl, const double *ysc, T 
                     int plane) {
   const Geom &g = c->g;
   prof_begin(c, KK_Z_RHS_FUSED);
-  if (sizeof(T) == 4 && fused_wide_ok(c)) {  // nz = 256, mixed form: the wide-row engine
+  if (fused_wide_ok(c)) {  // nz = 256: the wide-row engine
     IH_TRY(fused_wide_launch(c, d4, yfl, ysc, lap, p, rho, s6, gw, partials, nblocks_out, zsrc,
                              plane));
   } else {
@@ -2373,16 +2355,46 @@ static int autotune_t(Ctx *c) {
       rep += line;
     }
   }
+  // the fused z pass (nz = 256, mixed form): wide rows, or wide rows whose
+  // next input row is copied in with cp.async during the current transform
+  if (st == IH_OK && sizeof(T) == 4 && g.h == 128 && c->zwide) {
+    float tz[3] = {0.f, 0.f, 0.f};
+    T *lap = (T *)c->rbuf[0], *pz = (T *)c->rbuf[1];
+    for (int v = 1; v <= 2 && st == IH_OK; ++v) {
+      c->zwide = v;
+      int nblk = 0;
+      for (int r = 0; r <= reps && st == IH_OK; ++r) {
+        if (r == 1) cudaEventRecord(e0, c->stream);
+        st = fft_z_rhs_fused<T>(c, sp, (const T *)c->y.fl, c->y.sc, lap, pz, nullptr, sp,
+                                c->p.enable_gw, c->partials, &nblk, 1, 0);
+      }
+      if (st != IH_OK) break;
+      cudaEventRecord(e1, c->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&tz[v], e0, e1) != cudaSuccess) {
+        c->err = "autotune: event timing failed";
+        st = IH_ERR_CUDA;
+        break;
+      }
+      tz[v] /= reps;
+    }
+    if (st == IH_OK) {
+      c->zwide = tz[2] < tz[1] ? 2 : 1;
+      snprintf(line, sizeof line, "z pass wide %.1f us, wide+prefetch %.1f us; ", 1e3 * tz[1],
+               1e3 * tz[2]);
+      rep += line;
+    }
+  }
   c->prof_on = prof;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st != IH_OK) return st;
   snprintf(line, sizeof line,
            "chosen: x %s, y %s, deriv4-x %s, rt-x %s, rt-y %s, tensor %s, gw-yx slab %d, "
-           "gw planes %d",
+           "gw planes %d, z pass %d",
            variant_name(c->xy_var[0]), variant_name(c->xy_var[1]), variant_name(c->d4_var),
            variant_name(c->rt_var[0]), variant_name(c->rt_var[1]),
-           c->tensor_fused ? "fused" : "separate", c->gw_slab, c->gw_plane);
+           c->tensor_fused ? "fused" : "separate", c->gw_slab, c->gw_plane, c->zwide);
   c->tune_report = rep + line;
   return IH_OK;
 }

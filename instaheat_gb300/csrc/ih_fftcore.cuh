@@ -160,6 +160,26 @@ __device__ __forceinline__ T ksq(const Geom &g, int ia, int ja, int kz) {
   }
 }
 
+// one complex value global -> shared with cp.async (zero-filled when !valid)
+template <typename T>
+__device__ __forceinline__ void cp_async_c(C2<T> *s, const C2<T> *g, bool valid) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
+  if constexpr (sizeof(T) == 4) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(g),
+                 "r"(valid ? 8 : 0)
+                 : "memory");
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(g),
+                 "r"(valid ? 16 : 0)
+                 : "memory");
+  }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // energy density and pressure at one point (toolbox.c:172-250) from the
 // gradient dx, dy, dz, phi, dphi and psi.  FP64 form: full values.  Mixed form
 // (MIXED): the arguments are fluctuations about the FP64 homogeneous parts

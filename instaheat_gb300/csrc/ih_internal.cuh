@@ -199,7 +199,6 @@ struct Ctx {
   double hist_dt[4] = {0, 0, 0, 0}, hist_err[4] = {0, 0, 0, 0};
   int hist_n = 0;
   ih_mlp *proposer = nullptr;
-  int proposer_policy = 0;  // IH_PROPOSER_CLAMPED or IH_PROPOSER_CAP
   float *feat_dev = nullptr;    // 16 floats: 12 features, output at [12]
   double dt_next_pi = 0.0;      // the controller's own proposal of the last step
 
@@ -233,7 +232,7 @@ struct Ctx {
   int gw_tt_clusters = 0;  // resident clusters of k_gw_tt_plane
   int *waitflag = nullptr;  // device int: a bounded device-side wait timed out
   void *gwbuf = nullptr;    // plane-major tensor sources: 6 spectra of M complex (T)
-  int zwide = 1;         // the wide-row fused z pass where it applies (nz = 256, mixed)
+  int zwide = 1;         // the wide-row z passes where they apply (nz = 256)
   int gw_slab = 0;       // kz slab width of the tensor sources' y/x passes (0: whole arrays)
   int stage_fusion = 0;  // DOPRI853 stage inputs formed by the RHS of the previous stage
   int velocity_form = 1; // mixed form: stage combinations from the velocity halves only
@@ -318,10 +317,11 @@ template <typename T>
 int fft_z_rhs_fused(Ctx *c, const C2<T> *d4, const T *yfl, const double *ysc,
                     T *lap, T *p, T *rho, C2<T> *s6, int gw, double *partials,
                     int *nblocks_out, int zsrc, int plane = 0);
-// The same pass on the wide-row engine (ih_zwide.cu): mixed form, nz = 256.
+// The same pass on the wide-row engine (ih_zwide.cu): nz = 256, in the
+// context's precision (FP32 mixed form or FP64).
 bool fused_wide_ok(const Ctx *c);
 // the plain r2c z pass on the wide-row engine (same condition)
-int zr2c_wide_launch(Ctx *c, const float *in, long long istride, void *out, long long ostride,
+int zr2c_wide_launch(Ctx *c, const void *in, long long istride, void *out, long long ostride,
                      int count);
 int fused_wide_launch(Ctx *c, const void *d4, const void *yfl, const double *ysc, void *lap,
                       void *p, void *rho, void *s6, int gw, double *partials, int *nblk_out,

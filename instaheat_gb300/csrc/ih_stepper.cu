@@ -889,7 +889,32 @@ int step_features(Ctx *c, float *out) {
   return IH_OK;
 }
 
-// the learned proposal for the next step (after an accepted step)
+// the reference controller's next step after an accepted try of error err
+// (success(), dopri853.c:505-530): the scale safe err^-alpha err_old^beta in
+// [minscale, maxscale], not above 1 right after a rejection, then the Hubble
+// cap
+static double controller_next(const ih_dopri_cfg &g, double err, double err_old,
+                              bool after_reject, double dt, double rho_mean) {
+  const double alpha = 1.0 / 8.0 - g.beta * 0.2;
+  double scale;
+  if (err == 0.0) {
+    scale = g.maxscale;
+  } else {
+    scale = g.safe * pow(err, -alpha) * pow(err_old, g.beta);
+    if (scale < g.minscale) scale = g.minscale;
+    if (scale > g.maxscale) scale = g.maxscale;
+  }
+  double next = after_reject ? dt * fmin(scale, 1.0) : dt * scale;
+  if (g.max_dt_hubble_fraction > 0.0) {
+    const double minstep = g.max_dt_hubble_fraction * sqrt(3.0 / rho_mean);
+    if (next > minstep) next = minstep;
+  }
+  return next;
+}
+
+// the learned proposal for the next step (after an accepted step): the
+// network's log dt, clamped to [minscale, maxscale] x the step just taken and
+// to the Hubble cap
 static int learned_dt(Ctx *c, double dt_did, double rho_mean, double *dt_out) {
   float f[IH_MLP_INPUTS];
   IH_TRY(step_features(c, f));
@@ -902,12 +927,8 @@ static int learned_dt(Ctx *c, double dt_did, double rho_mean, double *dt_out) {
   double dt = exp((double)ylog);
   if (!(dt > 0.0) || !isfinite(dt)) dt = c->dt_next_pi;  // fall back to the controller
   dt = fmin(fmax(dt, dt_did * c->cfg.minscale), dt_did * c->cfg.maxscale);
-  if (c->cfg.max_dt_hubble_fraction > 0.0) {
-    // success() caps dt_next_pi with the same expression, so the comparison
-    // is exact where the controller sits on the cap
-    const double cap = c->cfg.max_dt_hubble_fraction * sqrt(3.0 / rho_mean);
-    dt = (c->proposer_policy == IH_PROPOSER_CAP && c->dt_next_pi >= cap) ? cap : fmin(dt, cap);
-  }
+  if (c->cfg.max_dt_hubble_fraction > 0.0)
+    dt = fmin(dt, c->cfg.max_dt_hubble_fraction * sqrt(3.0 / rho_mean));
   *dt_out = dt;
   return IH_OK;
 }
@@ -1282,25 +1303,13 @@ static int post_step_rhs(Ctx *c, double t, int want_output) {
 static int success(Ctx *c, double err, double rho_mean, double *dt) {
   const ih_dopri_cfg &g = c->cfg;
   const double alpha = 1.0 / 8.0 - g.beta * 0.2;
-  double scale;
   if (err <= 1.0) {
-    if (err == 0.0) {
-      scale = g.maxscale;
-    } else {
-      scale = g.safe * pow(err, -alpha) * pow(c->err_old, g.beta);
-      if (scale < g.minscale) scale = g.minscale;
-      if (scale > g.maxscale) scale = g.maxscale;
-    }
-    c->dt_next = c->reject ? (*dt) * fmin(scale, 1.0) : (*dt) * scale;
-    if (g.max_dt_hubble_fraction > 0.0) {
-      const double minstep = g.max_dt_hubble_fraction * sqrt(3.0 / rho_mean);
-      if (c->dt_next > minstep) c->dt_next = minstep;
-    }
+    c->dt_next = controller_next(g, err, c->err_old, c->reject != 0, *dt, rho_mean);
     c->err_old = fmax(err, 1.0e-4);
     c->reject = 0;
     return 1;
   }
-  scale = fmax(g.safe * pow(err, -alpha), g.minscale);
+  const double scale = fmax(g.safe * pow(err, -alpha), g.minscale);
   (*dt) *= scale;
   c->reject = 1;
   return 0;

@@ -21,7 +21,6 @@ PREC_F64 = 0
 PREC_MIXED = 1
 FFT_STOCKHAM, FFT_TWOSTEP, FFT_TWOSTEP_HALF, FFT_PIPELINED, FFT_THREESTEP = 0, 1, 2, 3, 4
 FFT_TWOSTEP_HALF_OCC = 5
-PROPOSER_CLAMPED, PROPOSER_CAP = 0, 1
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed",
           4: "call out of order", 5: "step size underflow", 6: "non-finite value"}
@@ -145,7 +144,6 @@ def load(build_if_missing: bool = True):
     L.ih_mlp_train.argtypes = [vp, _fp, _fp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_uint, _fp]
     L.ih_step_features.argtypes = [vp, _fp]
     L.ih_dopri853_set_proposer.argtypes = [vp, vp]
-    L.ih_dopri853_set_proposer_policy.argtypes = [vp, C.c_int]
     L.ih_dopri853_error_breakdown.argtypes = [vp, _dp]
     L.ih_dopri853_init_ex.argtypes = [vp, C.POINTER(DopriCfg), C.c_double, C.c_double, C.c_int]
     L.ih_mean_host.argtypes = [vp, _dp, C.c_size_t, _dp]
@@ -661,12 +659,6 @@ class Context:
         self._proposer = mlp  # keep it alive while the context uses it
         self._ck(self.L_.ih_dopri853_set_proposer(self.h, mlp.h if mlp is not None else None),
                  "ih_dopri853_set_proposer")
-
-    def set_proposer_policy(self, policy):
-        """PROPOSER_CLAMPED (0, the default) or PROPOSER_CAP (1: the Hubble cap
-        wherever the controller's own proposal is the cap)."""
-        self._ck(self.L_.ih_dopri853_set_proposer_policy(self.h, policy),
-                 "ih_dopri853_set_proposer_policy")
 
     def set_noise_floor(self, eta):
         self._ck(self.L_.ih_dopri853_set_noise_floor(self.h, eta), "ih_dopri853_set_noise_floor")

@@ -1,25 +1,31 @@
 """The learned step-size proposer: step logs, GPU training, model files.
 
-Why it exists: the mixed-precision form's DOPRI853 error estimate carries FP32
-round-off, so its controller alone does not reproduce the FP64 form's step
-sequence, and the reference's per-step spectral filter makes the GW spectrum
-depend on that sequence.  The proposer is trained to propose the FP64 form's
-next step size from what the mixed form itself observes; DOPRI853 still
-accepts or rejects every try and the reference controller handles rejections.
+Why it exists: the mixed-precision form's DOPRI853 error estimate is mostly
+below FP32 resolution at rtol = atol = 1e-8 (the embedded error of a step is
+far smaller than the FP32 rounding of the stage sums it is formed from, and
+the noise floor that keeps round-off from rejecting steps removes it), so its
+controller alone does not reproduce the FP64 form's step sequence, and the
+reference's per-step spectral filter makes the solution depend on that
+sequence (the filter is applied once per accepted step, so the number of
+steps sets how strongly the highest modes are damped).  The proposer is
+trained to propose the FP64 form's next step size from what the mixed form
+itself observes; DOPRI853 still accepts or rejects every try and the
+reference controller handles rejections.
 
-Step logs: for each seed, the FP64 form runs with its own controller and logs
-its accepted step sizes; the mixed form then replays exactly those steps and
-records, after every step, its feature vector (ih_step_features: last four
-log dt, last four log error norms, log a, H, log rms delta phi, log rms
-delta psi).  Training pairs: features after step n -> log dt_{n+1} of FP64.
+Step logs: for each run, the FP64 form runs with its own controller and logs
+its accepted steps (t, dt, err, tries); the mixed form then replays exactly
+those steps and records, after every step, its feature vector
+(ih_step_features: last four log dt, last four log error norms, log a, H,
+log rms delta phi, log rms delta psi).  Training pairs: features after step
+n -> log dt_{n+1} of FP64.
 
-    python -m instaheat_gb300.learned_dt --runs 128:1:20:1.0,128:2:10:0.8 --t-end 300 \\
-        --out instaheat_gb300/data/dt_mlp.json
+    python -m instaheat_gb300.learned_dt --n 128,256 --seeds 1,2,3 --t-end 1.0 \\
+        --out instaheat_gb300/data/dt_mlp.json [--save-data logs.npz]
+    python -m instaheat_gb300.learned_dt --from-data logs.npz --out model.json
 
-Each run is grid:seed:box:phi0 (box L in units of 1/m, phi0 the homogeneous
-field); the logs span the whole run, so the proposer sees the early phase
-(the error controller sets dt) and the late phase (the Hubble-fraction cap
-sets it, dopri853.c:525-530).
+Runs are given as grids x seeds (box 20/m, phi0 = 1) or, with --runs, as
+grid:seed:box:phi0 entries (box L in units of 1/m, phi0 the homogeneous
+field).
 """
 from __future__ import annotations
 
@@ -33,10 +39,12 @@ import numpy as np
 from . import gpu
 
 DEFAULT_MODEL = Path(__file__).resolve().parent / "data" / "dt_mlp.json"
+FORMAT = "instaheat_gb300 dt proposer v1"
 
 
 def step_log(n, seed, t_end, rtol=1e-8, device=0, amp=1e-3, L=20.0, phi0=1.0):
-    """(X, Y, info) for one realization: mixed-form features replaying FP64."""
+    """(X, Y, info, log64) for one realization: mixed-form features replaying
+    FP64, targets log dt of the FP64 run's next step, and the FP64 step log."""
     c64 = gpu.Context(n=(n,) * 3, L=(L,) * 3, precision=gpu.PREC_F64, device=device)
     c64.ic(seed=seed, amp=amp, phi0=phi0)
     c64.dopri_init(gpu.dopri_cfg(rtol, rtol), 0.0, 1e-3)
@@ -61,7 +69,7 @@ def step_log(n, seed, t_end, rtol=1e-8, device=0, amp=1e-3, L=20.0, phi0=1.0):
     cm.close()
     return (np.array(X, dtype=np.float32).reshape(-1, gpu.MLP_INPUTS), np.array(Y, dtype=np.float32),
             {"n": n, "seed": seed, "L": L, "phi0": phi0, "t_end": t_end, "steps_f64": int(steps),
-             "replayed": replayed, "wall_f64_s": w64})
+             "replayed": replayed, "wall_f64_s": w64}, log)
 
 
 def fit(X, Y, device=0, iters=3000, lr=3e-3, seed=1):
@@ -76,7 +84,7 @@ def fit(X, Y, device=0, iters=3000, lr=3e-3, seed=1):
 
 def save(mlp, path, meta=None):
     m, s, om, osd = mlp.norm
-    d = {"format": "instaheat_gb300 dt proposer v1", "params": [float(x) for x in mlp.params],
+    d = {"format": FORMAT, "params": [float(x) for x in mlp.params],
          "in_mean": [float(x) for x in m], "in_std": [float(x) for x in s],
          "out_mean": om, "out_std": osd, "meta": meta or {}}
     Path(path).parent.mkdir(parents=True, exist_ok=True)
@@ -85,6 +93,9 @@ def save(mlp, path, meta=None):
 
 def load(path=DEFAULT_MODEL, device=0):
     d = json.loads(Path(path).read_text())
+    if d.get("format") != FORMAT:
+        raise ValueError(f"{path}: a model of format {d.get('format')!r}; this library reads "
+                         f"{FORMAT!r}")
     mlp = gpu.MLP(device=device)
     mlp.params = np.array(d["params"], dtype=np.float32)
     mlp.set_norm(np.array(d["in_mean"]), np.array(d["in_std"]), d["out_mean"], d["out_std"])
@@ -150,30 +161,42 @@ def main(argv=None):
     ap.add_argument("--iters", type=int, default=3000)
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--out", default=str(DEFAULT_MODEL))
+    ap.add_argument("--save-data", default=None, help="write the step logs and pairs (.npz)")
+    ap.add_argument("--from-data", default=None, help="train on saved step logs (.npz)")
     args = ap.parse_args(argv)
     if args.evaluate:
         print(json.dumps(evaluate(args.eval_n, args.eval_seed, args.eval_t, args.out)), flush=True)
         return
-    Xs, Ys, infos = [], [], []
-    if args.runs:
-        runs = [(int(a), int(b), float(c), float(d))
-                for a, b, c, d in (r.split(":") for r in args.runs.split(","))]
+    if args.from_data:
+        z = np.load(args.from_data)
+        X, Y = z["X"], z["Y"]
+        infos = json.loads(str(z["infos"]))
     else:
-        runs = [(int(n), int(sd), 20.0, 1.0) for n in args.n.split(",")
-                for sd in args.seeds.split(",")]
-    for n, sd, L, phi0 in runs:
-        X, Y, info = step_log(n, sd, args.t_end, L=L, phi0=phi0)
-        print(json.dumps(info), flush=True)
-        Xs.append(X)
-        Ys.append(Y)
-        infos.append(info)
-    X = np.concatenate(Xs)
-    Y = np.concatenate(Ys)
+        Xs, Ys, infos, logs = [], [], [], []
+        if args.runs:
+            runs = [(int(a), int(b), float(c), float(d))
+                    for a, b, c, d in (r.split(":") for r in args.runs.split(","))]
+        else:
+            runs = [(int(n), int(sd), 20.0, 1.0) for n in args.n.split(",")
+                    for sd in args.seeds.split(",")]
+        for n, sd, L, phi0 in runs:
+            X, Y, info, log = step_log(n, sd, args.t_end, L=L, phi0=phi0)
+            print(json.dumps(info), flush=True)
+            Xs.append(X)
+            Ys.append(Y)
+            infos.append(info)
+            logs.append(log)
+        X = np.concatenate(Xs)
+        Y = np.concatenate(Ys)
+        if args.save_data:
+            np.savez(args.save_data, X=X, Y=Y, infos=json.dumps(infos),
+                     rows=np.array([len(x) for x in Xs]), **{f"log{i}": lg for i, lg in enumerate(logs)})
     mlp, hist = fit(X, Y, iters=args.iters, lr=args.lr)
     pred = mlp.forward(X)
     rms = float(np.sqrt(np.mean((pred - Y) ** 2)))
-    meta = {"rows": int(len(X)), "runs": infos, "t_end": args.t_end, "iters": args.iters,
-            "lr": args.lr, "final_loss": float(hist[-50:].mean()), "rms_log_dt_error": rms}
+    meta = {"rows": int(len(X)), "runs": infos, "t_end": infos[0]["t_end"] if infos else None,
+            "iters": args.iters, "lr": args.lr, "final_loss": float(hist[-50:].mean()),
+            "rms_log_dt_error": rms}
     save(mlp, args.out, meta)
     print(json.dumps({"saved": args.out, "rows": len(X), "loss_first": float(hist[:50].mean()),
                       "loss_last": float(hist[-50:].mean()), "rms_log_dt_error": rms}), flush=True)

@@ -69,29 +69,23 @@ def test_learned_proposer_gain_over_controller_alone(gpu_mod):
                                                                        r["f64"]["steps"]), r
 
 
-def test_proposer_policy_cap(gpu_mod):
-    """IH_PROPOSER_CAP: where the controller's own proposal is the Hubble cap
-    the next step is the cap, otherwise the proposal.  A proposer that always
-    proposes dt = 1e-3 (zero weights, output mean log 1e-3) at a cap of about
-    1.9e-3 (MAX_DT_HUBBLE_FRACTION = 1e-3 at <rho> ~ 0.83): the clamped policy
-    keeps every step at 1e-3; with the cap policy the controller, which would
-    grow the step past the cap, puts it on the cap."""
+def test_proposal_replaces_the_controller_step(gpu_mod):
+    """After each accepted step the proposal (the network's log dt) replaces
+    the controller's next step, clamped to [minscale, maxscale] x dt and to
+    the Hubble cap: a network that always proposes 2e-3 (zero weights, output
+    mean log 2e-3) makes every step after the first 2e-3, below the cap of
+    about 1.9e-2; DOPRI853 still accepts each try on its own error estimate."""
     mlp = gpu_mod.MLP(seed=1)
     mlp.params = np.zeros_like(mlp.params)
-    mlp.set_norm(np.zeros(12, np.float32), np.ones(12, np.float32), float(np.log(1e-3)), 1.0)
-    dts = {}
-    for policy in (gpu_mod.PROPOSER_CLAMPED, gpu_mod.PROPOSER_CAP):
-        ctx = gpu_mod.Context(n=(32, 32, 32), precision=gpu_mod.PREC_MIXED)
-        ctx.ic(seed=0, amp=1e-3)
-        ctx.dopri_init(gpu_mod.dopri_cfg(1e-8, 1e-8, max_dt_hubble_fraction=1e-3), 0.0, 1e-3)
-        ctx.set_proposer(mlp)
-        ctx.set_proposer_policy(policy)
-        _, log = ctx.dopri_run(0.05, log_cap=1000)
-        dts[policy] = log[:, 1]
-        with pytest.raises(gpu_mod.IHError):
-            ctx.set_proposer_policy(2)
-        ctx.close()
-    clamped, cap = dts[gpu_mod.PROPOSER_CLAMPED], dts[gpu_mod.PROPOSER_CAP]
-    # FP32 network output: exp(log 1e-3) to 1e-6; the last step lands on t = 0.05
-    np.testing.assert_allclose(clamped[:-1], 1e-3, rtol=1e-6)
-    assert np.all(cap[1:-1] > 1.5e-3) and np.all(cap[1:-1] < 2.5e-3), cap
+    mlp.set_norm(np.zeros(12, np.float32), np.ones(12, np.float32), float(np.log(2e-3)), 1.0)
+    ctx = gpu_mod.Context(n=(32, 32, 32), precision=gpu_mod.PREC_MIXED)
+    ctx.ic(seed=0, amp=1e-3)
+    ctx.dopri_init(gpu_mod.dopri_cfg(1e-8, 1e-8), 0.0, 1e-3)
+    ctx.set_proposer(mlp)
+    _, log = ctx.dopri_run(0.03, log_cap=1000)
+    ctx.close()
+    dts, tries = log[:, 1], log[:, 3]
+    assert log.shape[0] >= 10 and np.all(tries == 1), log
+    assert dts[0] == 1e-3
+    # FP32 network output: exp(log 2e-3) to 1e-6 relative; the last step lands on t = 0.03
+    np.testing.assert_allclose(dts[1:-1], 2e-3, rtol=1e-6)

@@ -619,6 +619,50 @@ def test_rhs_f64_parity_configured_sizes(gpu_mod, oracle_mod, n):
     o.close()
 
 
+@pytest.mark.parametrize("zwide", [1, 0])
+def test_rhs_f64_256_z_engines(gpu_mod, oracle_mod, zwide):
+    """Plain FP64 mk_rhs at 256^3 without filter and output (the derivative
+    round trips, the z spectrum of phi and the fused z pass taking d/dz from
+    it) on the wide-row z engine (8 lanes x 16 values per row, all butterflies
+    in registers; the default at nz = 256) and on the warp-per-row engine,
+    within 1e-11 of each segment of the oracle."""
+    n = (256, 256, 256)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_F64)
+    ctx.set_engine(6, zwide)
+    assert ctx.engines()[6] == zwide
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=7)
+    r_ref, _ = o.rhs(f, filter=0, output=0)
+    r_gpu, _ = ctx.mk_rhs(f, filter=0, output=0)
+    errs = seg_rel_err(r_gpu, r_ref, o.N, o.Next)
+    assert max(errs.values()) < 1e-11, errs
+    ctx.close()
+    o.close()
+
+
+def test_mixed_z_prefetch_is_bit_identical(gpu_mod, oracle_mod):
+    """Mixed form at 256^3: the wide-row z pass whose next input row is copied
+    in with cp.async (pass 6 engine 2) gives the same RHS to the bit as the
+    plain wide-row pass (engine 1), with and without the round trips; engine 2
+    is refused in the FP64 form."""
+    n = (256, 256, 256)
+    ctx = gpu_mod.Context(n=n, precision=gpu_mod.PREC_MIXED)
+    o = oracle_mod.Oracle(n=n)
+    f = make_state(o, seed=9, amp=1e-3, hamp=1e-6)
+    o.close()
+    for flags in ((0, 0), (1, 1)):
+        out = {}
+        for zw in (1, 2):
+            ctx.set_engine(6, zw)
+            out[zw], _ = ctx.mk_rhs(f, filter=flags[0], output=flags[1])
+        assert np.array_equal(out[1], out[2]), flags
+    ctx.close()
+    c64 = gpu_mod.Context(n=(32, 32, 32), precision=gpu_mod.PREC_F64)
+    with pytest.raises(gpu_mod.IHError):
+        c64.set_engine(6, 2)
+    c64.close()
+
+
 def test_dopri853_f64_to_t10(gpu_mod, oracle_mod):
     """32^3 FP64 DOPRI853 at rtol = atol = 1e-10 from t = 0 to t = 10/m (the
     reference's run loop: the last step clamped onto tf): the same accepted
