@@ -243,7 +243,8 @@ def bench_form(gpu, precision, device, seed, steps, warmup, profile=False, clock
            "fft_engines": dict(zip(("x", "y", "deriv4_x", "roundtrip_x", "roundtrip_y"),
                                    (ENGINE_NAMES[e] for e in ctx.engines()[:5])))
                           | {"tensor_x": ("fused" if ctx.engines()[5] else "separate"),
-                             "z_fused": ("wide rows" if ctx.engines()[6] else "warp rows"),
+                             "z_fused": ("warp rows", "wide rows",
+                                         "wide rows, next row prefetched")[ctx.engines()[6]],
                              "gw_yx_slab": ctx.engines()[7],
                              "gw_planes": ("persistent planes", "planes", "rows")[
                                  2 - ctx.engines()[8]]},
