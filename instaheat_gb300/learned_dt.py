@@ -26,6 +26,15 @@ n -> log dt_{n+1} of FP64.
 Runs are given as grids x seeds (box 20/m, phi0 = 1) or, with --runs, as
 grid:seed:box:phi0 entries (box L in units of 1/m, phi0 the homogeneous
 field).
+
+Replayed FP64 trajectories only show the network states on that trajectory,
+where "keep the last step" is nearly right; once its own proposals move the
+mixed form off it, nothing in the data says how to come back.  --dagger R
+adds R rounds of data from the mixed form running on the current proposer:
+before each of its steps the state is handed to an FP64 context, which takes
+the same step from it with the reference controller; the pair is (the mixed
+form's features after its step, log of the FP64 controller's next step).
+After each round the network is retrained on all pairs.
 """
 from __future__ import annotations
 
@@ -70,6 +79,60 @@ def step_log(n, seed, t_end, rtol=1e-8, device=0, amp=1e-3, L=20.0, phi0=1.0):
     return (np.array(X, dtype=np.float32).reshape(-1, gpu.MLP_INPUTS), np.array(Y, dtype=np.float32),
             {"n": n, "seed": seed, "L": L, "phi0": phi0, "t_end": t_end, "steps_f64": int(steps),
              "replayed": replayed, "wall_f64_s": w64}, log)
+
+
+def dagger_log(n, seed, t_end, mlp, rtol=1e-8, device=0, amp=1e-3, L=20.0, phi0=1.0,
+               every=1, max_steps=5000):
+    """(X, Y, info) from the mixed form running on the proposer `mlp`: for
+    each of its steps (every `every`-th), the FP64 controller's next step
+    after the same step from the same state, paired with the mixed form's
+    features after its step.  At most max_steps mixed steps."""
+    cfg = gpu.dopri_cfg(rtol, rtol)
+    cm = gpu.Context(n=(n,) * 3, L=(L,) * 3, precision=gpu.PREC_MIXED, device=device)
+    cm.ic(seed=seed, amp=amp, phi0=phi0)
+    cm.dopri_init(cfg, 0.0, 1e-3)
+    cm.set_proposer(mlp)
+    c64 = gpu.Context(n=(n,) * 3, L=(L,) * 3, precision=gpu.PREC_F64, device=device)
+    X, Y = [], []
+    t, dt, k = 0.0, 1e-3, 0
+    t0 = time.perf_counter()
+    while t < t_end and k < max_steps:
+        last = t + dt * 1.0001 > t_end  # the step landing on t_end: no pair
+        if last:
+            dt = t_end - t
+        take = (k % every == 0) and not last
+        if take:
+            c64.set_state(cm.get_state(), t)
+            c64.dopri_init(cfg, t, dt)
+            dt64 = c64.dopri_step(dt).dt_next
+        info = cm.dopri_step(dt)
+        if take and info.tries == 1 and dt64 > 0:
+            X.append(cm.step_features())
+            Y.append(np.log(dt64))
+        t, dt, k = info.t, info.dt_next, k + 1
+    cm.close()
+    c64.close()
+    return (np.array(X, dtype=np.float32).reshape(-1, gpu.MLP_INPUTS), np.array(Y, dtype=np.float32),
+            {"n": n, "seed": seed, "L": L, "phi0": phi0, "t_end": t_end, "t_reached": t,
+             "mixed_steps": k, "pairs": len(X), "wall_s": time.perf_counter() - t0})
+
+
+def pairs_from_data(z):
+    """Training pairs of a saved step-log file: (X, Y) as saved when the file
+    holds log dt targets, else rebuilt from the FP64 step logs (rows k of a
+    run pair with log dt_{k+1}, the run's landing step excluded)."""
+    target = str(z["target"]) if "target" in z.files else ""
+    if target == "log_dt":
+        return z["X"], z["Y"]
+    X, Y, off = [], [], 0
+    for i, r in enumerate(z["rows"]):
+        dts = z[f"log{i}"][:, 1]
+        for k in range(int(r)):
+            if k + 1 < len(dts) - 1:
+                X.append(z["X"][off + k])
+                Y.append(np.log(dts[k + 1]))
+        off += int(r)
+    return np.array(X, dtype=np.float32), np.array(Y, dtype=np.float32)
 
 
 def fit(X, Y, device=0, iters=3000, lr=3e-3, seed=1):
@@ -163,20 +226,26 @@ def main(argv=None):
     ap.add_argument("--out", default=str(DEFAULT_MODEL))
     ap.add_argument("--save-data", default=None, help="write the step logs and pairs (.npz)")
     ap.add_argument("--from-data", default=None, help="train on saved step logs (.npz)")
+    ap.add_argument("--dagger", type=int, default=0, help="rounds on the proposer's own states")
+    ap.add_argument("--dagger-every", type=int, default=1)
+    ap.add_argument("--dagger-max-steps", type=int, default=3000)
     args = ap.parse_args(argv)
     if args.evaluate:
         print(json.dumps(evaluate(args.eval_n, args.eval_seed, args.eval_t, args.out)), flush=True)
         return
+    runs = None
+    if args.runs:
+        runs = [(int(a), int(b), float(c), float(d))
+                for a, b, c, d in (r.split(":") for r in args.runs.split(","))]
     if args.from_data:
         z = np.load(args.from_data)
-        X, Y = z["X"], z["Y"]
+        X, Y = pairs_from_data(z)
         infos = json.loads(str(z["infos"]))
+        if runs is None:
+            runs = [(i["n"], i["seed"], i["L"], i["phi0"]) for i in infos]
     else:
         Xs, Ys, infos, logs = [], [], [], []
-        if args.runs:
-            runs = [(int(a), int(b), float(c), float(d))
-                    for a, b, c, d in (r.split(":") for r in args.runs.split(","))]
-        else:
+        if runs is None:
             runs = [(int(n), int(sd), 20.0, 1.0) for n in args.n.split(",")
                     for sd in args.seeds.split(",")]
         for n, sd, L, phi0 in runs:
@@ -189,12 +258,30 @@ def main(argv=None):
         X = np.concatenate(Xs)
         Y = np.concatenate(Ys)
         if args.save_data:
-            np.savez(args.save_data, X=X, Y=Y, infos=json.dumps(infos),
+            np.savez(args.save_data, X=X, Y=Y, infos=json.dumps(infos), target="log_dt",
                      rows=np.array([len(x) for x in Xs]), **{f"log{i}": lg for i, lg in enumerate(logs)})
     mlp, hist = fit(X, Y, iters=args.iters, lr=args.lr)
+    t_end = infos[0]["t_end"] if infos else args.t_end
+    for rnd in range(args.dagger):
+        for n, sd, L, phi0 in runs:
+            Xd, Yd, info = dagger_log(n, sd, t_end, mlp, L=L, phi0=phi0, every=args.dagger_every,
+                                      max_steps=args.dagger_max_steps)
+            info["round"] = rnd
+            print(json.dumps(info), flush=True)
+            infos.append(info)
+            X = np.concatenate([X, Xd])
+            Y = np.concatenate([Y, Yd])
+        mlp.close()
+        mlp, hist = fit(X, Y, iters=args.iters, lr=args.lr)
+        if rnd + 1 < args.dagger:  # the model of each intermediate round, for comparison
+            save(mlp, args.out.replace(".json", f"_round{rnd}.json"),
+                 {"rows": int(len(X)), "dagger_rounds": rnd + 1})
+        if args.save_data:
+            np.savez(args.save_data.replace(".npz", f"_dagger{rnd}.npz"), X=X, Y=Y,
+                     infos=json.dumps(infos), target="log_dt")
     pred = mlp.forward(X)
     rms = float(np.sqrt(np.mean((pred - Y) ** 2)))
-    meta = {"rows": int(len(X)), "runs": infos, "t_end": infos[0]["t_end"] if infos else None,
+    meta = {"rows": int(len(X)), "runs": infos, "t_end": t_end, "dagger_rounds": args.dagger,
             "iters": args.iters, "lr": args.lr, "final_loss": float(hist[-50:].mean()),
             "rms_log_dt_error": rms}
     save(mlp, args.out, meta)
