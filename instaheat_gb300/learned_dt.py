@@ -262,11 +262,12 @@ def main(argv=None):
                      rows=np.array([len(x) for x in Xs]), **{f"log{i}": lg for i, lg in enumerate(logs)})
     mlp, hist = fit(X, Y, iters=args.iters, lr=args.lr)
     t_end = infos[0]["t_end"] if infos else args.t_end
+    prior = len({i["round"] for i in infos if "round" in i})  # rounds already in --from-data
     for rnd in range(args.dagger):
         for n, sd, L, phi0 in runs:
             Xd, Yd, info = dagger_log(n, sd, t_end, mlp, L=L, phi0=phi0, every=args.dagger_every,
                                       max_steps=args.dagger_max_steps)
-            info["round"] = rnd
+            info["round"] = prior + rnd
             print(json.dumps(info), flush=True)
             infos.append(info)
             X = np.concatenate([X, Xd])
@@ -281,7 +282,8 @@ def main(argv=None):
                      infos=json.dumps(infos), target="log_dt")
     pred = mlp.forward(X)
     rms = float(np.sqrt(np.mean((pred - Y) ** 2)))
-    meta = {"rows": int(len(X)), "runs": infos, "t_end": t_end, "dagger_rounds": args.dagger,
+    meta = {"rows": int(len(X)), "runs": infos, "t_end": t_end,
+            "dagger_rounds": prior + args.dagger,
             "iters": args.iters, "lr": args.lr, "final_loss": float(hist[-50:].mean()),
             "rms_log_dt_error": rms}
     save(mlp, args.out, meta)
