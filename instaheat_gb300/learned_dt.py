@@ -241,8 +241,8 @@ def main(argv=None):
         z = np.load(args.from_data)
         X, Y = pairs_from_data(z)
         infos = json.loads(str(z["infos"]))
-        if runs is None:
-            runs = [(i["n"], i["seed"], i["L"], i["phi0"]) for i in infos]
+        if runs is None:  # the replayed runs of the file (not its earlier rounds)
+            runs = [(i["n"], i["seed"], i["L"], i["phi0"]) for i in infos if "round" not in i]
     else:
         Xs, Ys, infos, logs = [], [], [], []
         if runs is None:
