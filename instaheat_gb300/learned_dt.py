@@ -229,6 +229,10 @@ def main(argv=None):
     ap.add_argument("--dagger", type=int, default=0, help="rounds on the proposer's own states")
     ap.add_argument("--dagger-every", type=int, default=1)
     ap.add_argument("--dagger-max-steps", type=int, default=3000)
+    ap.add_argument("--dagger-t-end", type=float, default=None,
+                    help="end time of the rounds' runs (default: that of the replays)")
+    ap.add_argument("--dagger-repeat", type=int, default=1,
+                    help="weight of the rounds' pairs (each enters the training set this often)")
     args = ap.parse_args(argv)
     if args.evaluate:
         print(json.dumps(evaluate(args.eval_n, args.eval_seed, args.eval_t, args.out)), flush=True)
@@ -262,16 +266,18 @@ def main(argv=None):
                      rows=np.array([len(x) for x in Xs]), **{f"log{i}": lg for i, lg in enumerate(logs)})
     mlp, hist = fit(X, Y, iters=args.iters, lr=args.lr)
     t_end = infos[0]["t_end"] if infos else args.t_end
+    t_round = args.dagger_t_end if args.dagger_t_end is not None else t_end
     prior = len({i["round"] for i in infos if "round" in i})  # rounds already in --from-data
     for rnd in range(args.dagger):
         for n, sd, L, phi0 in runs:
-            Xd, Yd, info = dagger_log(n, sd, t_end, mlp, L=L, phi0=phi0, every=args.dagger_every,
+            Xd, Yd, info = dagger_log(n, sd, t_round, mlp, L=L, phi0=phi0, every=args.dagger_every,
                                       max_steps=args.dagger_max_steps)
             info["round"] = prior + rnd
+            info["repeat"] = args.dagger_repeat
             print(json.dumps(info), flush=True)
             infos.append(info)
-            X = np.concatenate([X, Xd])
-            Y = np.concatenate([Y, Yd])
+            X = np.concatenate([X] + [Xd] * args.dagger_repeat)
+            Y = np.concatenate([Y] + [Yd] * args.dagger_repeat)
         mlp.close()
         mlp, hist = fit(X, Y, iters=args.iters, lr=args.lr)
         if rnd + 1 < args.dagger:  # the model of each intermediate round, for comparison
